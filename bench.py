@@ -1,0 +1,333 @@
+#!/usr/bin/env python
+"""Checkers Monte Carlo playout throughput on GB300.
+
+Workload (one step): 64 seeded positions (seed 2016; each plays U{0..30}
+uniformly random legal plies from the start) x 4,096 uniformly random
+playouts = 262,144 playouts, int8 outcomes.  Each step uses fresh random
+streams (stream_base advances), so no step repeats work.
+
+  value  playouts/s of the playout kernel on device-resident inputs, summed
+         CUDA-event time of the K timed launches (L2 flushed between steps)
+  e2e    the same metric through the public C ABI call gpuai_playouts() on
+         host buffers: H2D of boards + offsets and D2H of outcomes every step
+  roofline  integer-issue roofline of the playout kernel
+  cpu_baseline  the reference's HostPlayoutDriver (built from its sources
+         where present, else the oracle's restatement of it) on the host's
+         cores, on a bounded sample of the same positions
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "checkers playouts/sec on 1 GB300 vs host CPU; win rate vs plain at equal ms/move"
+UNIT = "playouts/s"
+N_POS, REPS, POS_SEED, MAX_PLIES = 64, 4096, 2016, 30
+TOTAL = N_POS * REPS
+WORKLOAD = {
+    "workload": "uniform random playouts: 64 seeded positions (0-30 random plies, seed 2016) x 4096",
+    "positions": N_POS,
+    "playouts_per_position": REPS,
+    "playouts_per_step": TOTAL,
+    "policy": "random",
+    "l2": "flushed between steps (256 MiB write, outside the timed events)",
+}
+# Lane-instructions per ply of the playout kernel, frozen from the first
+# correct kernel's ncu capture (smsp__thread_inst_executed.sum / plies);
+# the algorithmic work unit of the integer-issue roofline.
+OPS_PER_PLY = 0.0
+# DRAM bytes per launch of the playout kernel from one ncu capture
+# (dram__bytes_read.sum + dram__bytes_write.sum); None until captured.
+TRAFFIC_BYTES = None
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except OSError:
+        return {"sm_max_mhz": 2070.0, "hbm_gbs": 6800.0}, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    NAMES = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+
+    def __init__(self, bus_id=None):
+        self.rows = []
+        self.proc = None
+        cmd = ["nvidia-smi", "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits", "-lms", "200"]
+        if bus_id:
+            cmd += ["-i", bus_id]
+        try:
+            self.proc = subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            return
+        self.t = threading.Thread(target=self._read, daemon=True)
+        self.t.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                self.rows.append(parts)
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.3)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        reasons = set()
+        for r in self.rows:
+            for name, v in zip(self.NAMES, r[5:9]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.rows)}
+
+
+def cpu_reference_runner():
+    """The reference's host playout path on this machine's cores.
+
+    Returns (run(states) -> outcomes, kind, threads).  kind "reference" is the
+    reference's own HostPlayoutDriver compiled from its sources (only where
+    those sources were present at build time and the objects match this
+    machine); otherwise "port", the oracle's line-by-line restatement of it.
+    """
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_lib as L  # the CPU baseline is the one product-external use of the oracle
+
+    threads = os.cpu_count() or 1
+    try:
+        if os.path.exists(L.REF_SO):
+            lib = L.ref()
+            if lib is not None:
+                return (lambda st: L.host_playouts_ref(st, srand_seed=1)), "reference", threads
+    except OSError:
+        pass
+    L.oracle()
+    return (lambda st: L.host_playouts_port(st, nthreads=threads, srand_seed=1)), "port", threads
+
+
+def time_cpu_baseline(positions, min_seconds=10.0, max_seconds=30.0):
+    run, kind, threads = cpu_reference_runner()
+    chunk = np.repeat(positions, 64, axis=0)  # 64 playouts per position per chunk
+    done, t0 = 0, time.perf_counter()
+    while True:
+        run(chunk)
+        done += len(chunk)
+        el = time.perf_counter() - t0
+        if el >= min_seconds or el >= max_seconds:
+            break
+    return {"value": done / el, "unit": UNIT, "cores": threads, "kind": kind,
+            "sample": f"{done} playouts ({done // len(positions)} per position) of the same 64 positions, "
+                      f"{el:.1f} s, HostPlayoutDriver (src/playout.cpp:17-32)"}
+
+
+def dist_setup(n_gpus):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("nccl" if os.environ.get("BENCH_GLOO") is None else "gloo")
+    return rank, world, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def run_reference(args):
+    rank, world, _ = dist_setup(args.gpus)
+    if rank != 0:
+        return
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_lib as L
+    positions = L.random_positions(POS_SEED, N_POS, 0, MAX_PLIES)
+    run, kind, threads = cpu_reference_runner()
+    per_pos = 256
+    states = np.repeat(positions, per_pos, axis=0)
+    for _ in range(args.warmup):
+        run(states)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        run(states)
+    el = time.perf_counter() - t0
+    value = args.steps * len(states) / el
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+        "config": dict(WORKLOAD, sample_per_step=f"{len(states)} playouts ({per_pos} per position)"),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": kind,
+                         "sample": f"{per_pos} playouts per position per step, HostPlayoutDriver "
+                                   "(src/playout.cpp:17-32)"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "gpu_launches": 0,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    rank, world, local = dist_setup(args.gpus)
+    import torch
+    from gpu_ai_gb300 import Engine
+
+    torch.cuda.set_device(local)
+    eng = Engine(local)
+    info = eng.device_info()
+    positions = eng.random_positions(POS_SEED, N_POS, 0, MAX_PLIES)
+    reps = np.full(N_POS, REPS, dtype=np.uint32)
+    d_pos = torch.from_numpy(positions.view(np.int32).copy()).cuda()
+    d_out = torch.empty(TOTAL, dtype=torch.int8, device="cuda")
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.current_stream()
+    sid = stream.cuda_stream
+    base = (rank << 40)
+
+    def step(k):
+        eng.playouts_device(d_pos.data_ptr(), None, N_POS, REPS, TOTAL, 0x5EED, base + k * TOTAL, 0,
+                            d_out.data_ptr(), sid)
+
+    for k in range(args.warmup):
+        flush.zero_()
+        step(k)
+    torch.cuda.synchronize()
+    st, _ = eng.status()
+    if st:
+        raise RuntimeError(f"kernel status {st}")
+
+    bus = None
+    try:
+        bus = torch.cuda.get_device_properties(local).pci_bus_id if hasattr(
+            torch.cuda.get_device_properties(local), "pci_bus_id") else None
+    except Exception:
+        bus = None
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    plies = 0
+    barrier(world)
+    torch.cuda.synchronize()
+    sampler = ClockSampler(bus)
+    wall0 = time.perf_counter()
+    for k in range(args.steps):
+        flush.zero_()
+        ev[k][0].record(stream)
+        step(args.warmup + k)
+        ev[k][1].record(stream)
+        st, pl = eng.status()  # synchronises; outside the event pair
+        if st:
+            raise RuntimeError(f"kernel status {st}")
+        plies += pl
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - wall0
+    barrier(world)
+    clocks = sampler.stop()
+    kern_s = sum(a.elapsed_time(b) for a, b in ev) / 1e3
+    kern_s_max = max_over_ranks(kern_s, world)
+    value = world * args.steps * TOTAL / kern_s_max
+
+    # ---- end to end through the public host-buffer call
+    h2d = N_POS * 16 + (N_POS + 1) * 4
+    d2h = TOTAL + 16
+    for k in range(2):
+        eng.playouts(positions, reps, seed=0xE2E, stream_base=base + k * TOTAL)
+    barrier(world)
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        out = eng.playouts(positions, reps, seed=0xE2E, stream_base=base + (k + 2) * TOTAL)
+    e2e_s = time.perf_counter() - t0
+    e2e_s = max_over_ranks(e2e_s, world)
+    assert out.shape == (TOTAL,)
+    e2e = {"value": world * args.steps * TOTAL / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
+           "d2h_bytes_per_step": d2h}
+
+    if rank != 0:
+        return
+    peaks, src = measured_peaks()
+    sm_mhz = float(peaks.get("sm_max_mhz", 2070.0))
+    peak_ops = info["sms"] * 128 * sm_mhz * 1e6  # lanes issued per second: SMs x 4 schedulers x 32 lanes
+    plies_s = plies / kern_s
+    roof = {"bound": "int_issue", "unit": "Tlane-op/s",
+            "peak": peak_ops / 1e12, "peak_source": f"{info['sms']} SMs x 128 lanes x {sm_mhz:.0f} MHz ({src})",
+            "ops_per_ply": OPS_PER_PLY, "plies_per_s": plies_s, "traffic": TRAFFIC_BYTES}
+    if OPS_PER_PLY:
+        roof["achieved"] = plies_s * OPS_PER_PLY / 1e12
+        roof["frac"] = roof["achieved"] / roof["peak"]
+        if clocks.get("sm_mhz"):
+            roof["frac_at_sampled_clock"] = roof["frac"] * sm_mhz / clocks["sm_mhz"]
+    else:
+        roof["achieved"] = None
+        roof["frac"] = None
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": kern_s / args.steps * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic (seeded positions)",
+        "config": dict(WORKLOAD, parallelism=f"replicas{world}" if world > 1 else "single"),
+        "plies_per_playout": plies / (args.steps * TOTAL),
+        "wall_ms_per_step": wall / args.steps * 1e3,
+        "gpu_launches": args.steps,
+        "e2e": e2e,
+        "roofline": roof,
+        "clocks": clocks,
+        "device": info,
+    }
+    if world == 1 and not args.no_cpu:
+        line["cpu_baseline"] = time_cpu_baseline(positions)
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("--warmup must be >= 3")
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

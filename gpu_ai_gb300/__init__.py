@@ -1,0 +1,32 @@
+"""GB300-native Monte Carlo playout engine for 8x8 checkers.
+
+The compute path is libgpuai.so (hand-written sm_103a CUDA kernels behind the
+C ABI in include/gpuai.h); :class:`Engine` is its Python binding.
+"""
+from .engine import (  # noqa: F401
+    ERR_CUDA,
+    ERR_INVALID,
+    ERR_LIMIT,
+    ERR_NO_DEVICE,
+    ERR_OOM,
+    OK,
+    POLICY_EPS_GREEDY,
+    POLICY_RANDOM,
+    POLICY_REF_HEURISTIC,
+    START_BOARD,
+    Engine,
+    GpuAIError,
+    header_symbols,
+    load_library,
+)
+
+__all__ = [
+    "Engine",
+    "GpuAIError",
+    "load_library",
+    "header_symbols",
+    "START_BOARD",
+    "POLICY_RANDOM",
+    "POLICY_REF_HEURISTIC",
+    "POLICY_EPS_GREEDY",
+]

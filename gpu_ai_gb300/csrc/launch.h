@@ -1,0 +1,41 @@
+// launch.h -- host-side launchers of the playout kernels (internal to libgpuai).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "rules.cuh"
+
+namespace ga {
+
+// Status bits written by the kernels (atomicOr into the status word).
+constexpr uint32_t kStatusDepth = 1u;     // capture sequence deeper than kMaxDepth
+constexpr uint32_t kStatusOverflow = 2u;  // move list longer than the caller's buffer
+constexpr uint32_t kStatusPlyCap = 4u;    // playout exceeded kMaxPlies (cannot happen under the 50-ply rule)
+
+constexpr int kPlayoutBlock = 256;
+constexpr uint32_t kMaxPlies = 4096;
+
+struct PlayoutArgs {
+  const Board *pos;
+  const uint32_t *offsets;  // npos+1 prefix sums, or nullptr for uniform repetitions
+  uint32_t npos;
+  uint32_t uniform_reps;
+  uint32_t total;
+  uint64_t seed;
+  uint64_t stream_base;
+  int8_t *out;
+  uint32_t *counter;              // work counter, zero before launch
+  uint32_t *status;               // status bits, zero before launch
+  unsigned long long *plies;      // plies played (optional)
+};
+
+// Resident blocks per SM of the playout kernel for `policy`.
+cudaError_t playout_occupancy(int policy, int *blocks_per_sm);
+cudaError_t launch_playouts(const PlayoutArgs &a, int policy, int grid, cudaStream_t s);
+cudaError_t launch_genmoves(const Board *pos, uint32_t n, void *out, uint32_t max_moves,
+                            uint8_t *counts, uint32_t *status, cudaStream_t s);
+cudaError_t launch_random_positions(uint64_t seed, uint32_t n, uint32_t min_plies,
+                                    uint32_t max_plies, Board *out, cudaStream_t s);
+
+}  // namespace ga

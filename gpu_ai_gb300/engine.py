@@ -1,0 +1,176 @@
+"""Python binding of libgpuai (include/gpuai.h) over ctypes.
+
+This is the reference-facing entry for Python callers and the test/bench
+harness: a batch of positions in, one int8 outcome per playout out
+(+1 PLAYER_1 won, -1 PLAYER_2 won, 0 drawn), mirroring
+``PlayoutDriver::runPlayouts`` (src/playout.hpp:27-33).  All computation runs
+in the CUDA kernels of libgpuai.so; there is no CPU path, and a missing or
+unbuilt library raises instead of falling back.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import re
+from typing import Optional, Tuple
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(PKG)
+LIB_PATH = os.path.join(PKG, "lib", "libgpuai.so")
+HEADER = os.path.join(ROOT, "include", "gpuai.h")
+
+POLICY_RANDOM = 0
+POLICY_REF_HEURISTIC = 1
+POLICY_EPS_GREEDY = 2
+
+OK = 0
+ERR_INVALID = -1
+ERR_CUDA = -2
+ERR_OOM = -3
+ERR_LIMIT = -4
+ERR_NO_DEVICE = -5
+
+START_BOARD = np.array([0x00000FFF, 0xFFF00000, 0, 0], dtype=np.uint32)
+
+_u32p = ctypes.POINTER(ctypes.c_uint32)
+_u8p = ctypes.POINTER(ctypes.c_uint8)
+_i8p = ctypes.POINTER(ctypes.c_int8)
+_i32p = ctypes.POINTER(ctypes.c_int32)
+_u64p = ctypes.POINTER(ctypes.c_uint64)
+
+_lib = None
+
+
+class GpuAIError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"gpuai error {code}: {msg}")
+        self.code = code
+
+
+def header_symbols() -> list:
+    """Function names declared in include/gpuai.h."""
+    src = open(HEADER).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(gpuai_[a-z_]+)\s*\(", src)))
+
+
+def load_library(path: str = LIB_PATH):
+    """Load libgpuai.so; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(f"{path} is missing: build it with gpu_ai_gb300.build.build()")
+    lib = ctypes.CDLL(path)
+    lib.gpuai_last_error.restype = ctypes.c_char_p
+    lib.gpuai_create.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)]
+    lib.gpuai_destroy.argtypes = [ctypes.c_void_p]
+    lib.gpuai_destroy.restype = None
+    lib.gpuai_playouts.argtypes = [ctypes.c_void_p, _u32p, _u32p, ctypes.c_uint32, ctypes.c_uint64,
+                                   ctypes.c_uint64, ctypes.c_int32, _i8p]
+    lib.gpuai_playouts_device.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32,
+                                          ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_uint64,
+                                          ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p]
+    lib.gpuai_status.argtypes = [ctypes.c_void_p, _u32p, _u64p]
+    lib.gpuai_genmoves.argtypes = [ctypes.c_void_p, _u32p, ctypes.c_uint32, _u8p, ctypes.c_uint32, _u8p]
+    lib.gpuai_random_positions.argtypes = [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint32,
+                                           ctypes.c_uint32, _u32p]
+    lib.gpuai_device_info.argtypes = [ctypes.c_void_p, _i32p, _i32p, _i32p]
+    for name in header_symbols():
+        if name not in ("gpuai_last_error", "gpuai_destroy"):
+            getattr(lib, name).restype = ctypes.c_int
+    _lib = lib
+    return lib
+
+
+def _check(rc: int):
+    if rc != OK:
+        raise GpuAIError(rc, load_library().gpuai_last_error().decode())
+
+
+def _boards(pos) -> np.ndarray:
+    a = np.ascontiguousarray(pos, dtype=np.uint32)
+    if a.ndim == 1:
+        a = a.reshape(-1, 4)
+    if a.ndim != 2 or a.shape[1] != 4:
+        raise ValueError("boards must have shape (n, 4): p1, p2, kings, meta")
+    return a
+
+
+class Engine:
+    """One libgpuai context (one CUDA stream) on `device`."""
+
+    def __init__(self, device: int = 0):
+        self.lib = load_library()
+        ctx = ctypes.c_void_p()
+        _check(self.lib.gpuai_create(device, ctypes.byref(ctx)))
+        self.ctx = ctx
+
+    def close(self):
+        if self.ctx:
+            self.lib.gpuai_destroy(self.ctx)
+            self.ctx = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def playouts(self, pos, reps=None, seed: int = 0, stream_base: int = 0,
+                 policy: int = POLICY_RANDOM) -> np.ndarray:
+        """reps[p] playouts from pos[p] (one each if reps is None); int8 outcomes in order."""
+        b = _boards(pos)
+        n = b.shape[0]
+        if reps is None:
+            total = n
+            rp = None
+        else:
+            r = np.ascontiguousarray(reps, dtype=np.uint32)
+            if r.shape != (n,):
+                raise ValueError("reps must have one entry per board")
+            total = int(r.sum(dtype=np.uint64))
+            rp = r.ctypes.data_as(_u32p)
+        out = np.empty(total, dtype=np.int8)
+        _check(self.lib.gpuai_playouts(self.ctx, b.ctypes.data_as(_u32p), rp, n, seed, stream_base, policy,
+                                       out.ctypes.data_as(_i8p)))
+        return out
+
+    def playouts_device(self, d_pos: int, d_offsets: Optional[int], npos: int, uniform_reps: int, total: int,
+                        seed: int, stream_base: int, policy: int, d_out: int, stream: Optional[int] = None):
+        """Enqueue playouts on device pointers (no synchronisation)."""
+        _check(self.lib.gpuai_playouts_device(self.ctx, d_pos, d_offsets, npos, uniform_reps, total, seed,
+                                              stream_base, policy, d_out, stream))
+
+    def status(self) -> Tuple[int, int]:
+        st = ctypes.c_uint32()
+        pl = ctypes.c_uint64()
+        _check(self.lib.gpuai_status(self.ctx, ctypes.byref(st), ctypes.byref(pl)))
+        return int(st.value), int(pl.value)
+
+    def genmoves(self, pos, max_moves: int = 64):
+        b = _boards(pos)
+        n = b.shape[0]
+        out = np.zeros((n, max_moves, 32), dtype=np.uint8)
+        counts = np.zeros(n, dtype=np.uint8)
+        _check(self.lib.gpuai_genmoves(self.ctx, b.ctypes.data_as(_u32p), n, out.ctypes.data_as(_u8p),
+                                       max_moves, counts.ctypes.data_as(_u8p)))
+        return out, counts
+
+    def random_positions(self, seed: int, n: int, min_plies: int, max_plies: int) -> np.ndarray:
+        out = np.zeros((n, 4), dtype=np.uint32)
+        _check(self.lib.gpuai_random_positions(self.ctx, seed, n, min_plies, max_plies, out.ctypes.data_as(_u32p)))
+        return out
+
+    def device_info(self):
+        a, b, c = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+        _check(self.lib.gpuai_device_info(self.ctx, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
+        return {"sms": a.value, "blocks_per_sm": b.value, "block_threads": c.value}

@@ -1,0 +1,109 @@
+/*
+ * gpuai.h -- C ABI of the GB300 checkers playout engine (libgpuai.so).
+ *
+ * Plain C types only: no CUDA or C++ types cross this boundary.  Every call
+ * returns a status (GPUAI_OK or a negative GPUAI_ERR_*); none exits the
+ * process.  gpuai_last_error() gives the message of the calling thread's last
+ * failure.
+ *
+ * Boards are 16-byte bitboard records over the 32 dark squares, square
+ * s = row*4 + col/2 (row 0 is PLAYER_1's back rank, dark squares are
+ * col = 1-(row%2), +2, ...).  Outcomes are int8: +1 PLAYER_1 won, -1 PLAYER_2
+ * won, 0 drawn.
+ *
+ * Threading: calls on one context are serialised by the context; use one
+ * context per host thread (each owns its own CUDA stream) for concurrency.
+ */
+#ifndef GPUAI_H
+#define GPUAI_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GPUAI_OK 0
+#define GPUAI_ERR_INVALID (-1)   /* bad argument or malformed board */
+#define GPUAI_ERR_CUDA (-2)      /* CUDA runtime error (message says which) */
+#define GPUAI_ERR_OOM (-3)       /* device or pinned allocation failed */
+#define GPUAI_ERR_LIMIT (-4)     /* a kernel hit an internal limit (status word) */
+#define GPUAI_ERR_NO_DEVICE (-5) /* no CUDA device, or the device index is out of range */
+
+#define GPUAI_POLICY_RANDOM 0        /* uniform over the legal move list */
+#define GPUAI_POLICY_REF_HEURISTIC 1 /* argmax of material-ratio weight + noise */
+#define GPUAI_POLICY_EPS_GREEDY 2    /* eps = 0.1 random, else greedy material+advancement */
+
+/* Board record.  meta: bit 0 = side to move (0 PLAYER_1, 1 PLAYER_2);
+ * bits 8..15 = plies since the last capture (>= 50 is a draw); other bits 0. */
+typedef struct gpuai_board {
+  uint32_t p1;    /* squares holding PLAYER_1 pieces */
+  uint32_t p2;    /* squares holding PLAYER_2 pieces */
+  uint32_t kings; /* squares holding kings (either side) */
+  uint32_t meta;
+} gpuai_board;
+
+/* One legal move, 32 bytes.  Unused path/removed slots are 0xFF. */
+typedef struct gpuai_move {
+  uint8_t from, to, jumps, promoted;
+  uint8_t path[12];    /* landing square of each jump, in order (last = to) */
+  uint8_t removed[12]; /* captured square of each jump, in order */
+  uint8_t pad[4];      /* zero */
+} gpuai_move;
+
+typedef struct gpuai_ctx gpuai_ctx;
+
+/* Create a context on CUDA device `device` with its own stream.
+ * Replaces the per-call cudaMalloc/stack-limit set-up of
+ * DeviceMultiplePlayoutDriver::runPlayouts (src/multiplePlayout.cu:53-98). */
+int gpuai_create(int device, gpuai_ctx **out);
+void gpuai_destroy(gpuai_ctx *ctx);
+
+/* Message of the calling thread's last failed call ("" if none). */
+const char *gpuai_last_error(void);
+
+/* Run playouts from host buffers: reps[p] playouts from pos[p] (reps NULL
+ * means one each), outcomes written in order to out (sum of reps entries).
+ * Playout j (0-based over the whole call) uses random stream id
+ * stream_base + j under `seed`.  npos == 0 returns GPUAI_OK without a launch.
+ * Replaces PlayoutDriver::runPlayouts (src/playout.hpp:27-33) as implemented
+ * by DeviceMultiplePlayoutDriver / DeviceSinglePlayoutDriver /
+ * DeviceCoarsePlayoutDriver / DeviceHeuristicPlayoutDriver
+ * (src/multiplePlayout.cu:53-98, src/singlePlayout.cu:71-120,
+ * src/coarsePlayout.cu:91-163, src/heuristicPlayout.cu:102-147). */
+int gpuai_playouts(gpuai_ctx *ctx, const gpuai_board *pos, const uint32_t *reps, uint32_t npos,
+                   uint64_t seed, uint64_t stream_base, int32_t policy, int8_t *out);
+
+/* Same work on device-resident buffers, enqueued on `stream` (a cudaStream_t,
+ * or NULL for the context's stream) without synchronising.  d_offsets holds
+ * npos+1 exclusive prefix sums of the repetitions, or is NULL when every
+ * position has `uniform_reps` playouts.  total = number of playouts.  Calls on
+ * one context must be ordered on one stream: they share the context's work
+ * counter.  Check gpuai_status() after synchronising. */
+int gpuai_playouts_device(gpuai_ctx *ctx, const gpuai_board *d_pos, const uint32_t *d_offsets,
+                          uint32_t npos, uint32_t uniform_reps, uint32_t total, uint64_t seed,
+                          uint64_t stream_base, int32_t policy, int8_t *d_out, void *stream);
+
+/* Status word and ply count of the last device-side playout launch (reads
+ * device memory; synchronises the context's stream).  status 0 = fine. */
+int gpuai_status(gpuai_ctx *ctx, uint32_t *status, uint64_t *plies);
+
+/* Legal move lists of n boards, in the reference's State::genMoves order
+ * (src/state.cu:239-245): out[i*max_moves + k], counts[i] = number of moves.
+ * Returns GPUAI_ERR_LIMIT if some list is longer than max_moves. */
+int gpuai_genmoves(gpuai_ctx *ctx, const gpuai_board *pos, uint32_t n, gpuai_move *out,
+                   uint32_t max_moves, uint8_t *counts);
+
+/* n seeded positions: position i plays U{min_plies..max_plies} uniformly random
+ * legal plies from the standard start (stopping early at a finished game).
+ * Replaces genRandomStates (src/driver.cpp:76-104). */
+int gpuai_random_positions(gpuai_ctx *ctx, uint64_t seed, uint32_t n, uint32_t min_plies,
+                           uint32_t max_plies, gpuai_board *out);
+
+/* Number of SMs and resident playout blocks per SM chosen for this device. */
+int gpuai_device_info(gpuai_ctx *ctx, int32_t *sms, int32_t *blocks_per_sm, int32_t *block_threads);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GPUAI_H */

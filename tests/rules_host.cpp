@@ -1,0 +1,82 @@
+// rules_host.cpp -- host build of the device rules header, for CPU tests only.
+//
+// gpu_ai_gb300/csrc/rules.cuh is written __host__ __device__; compiling it
+// with g++ lets the CPU test suite check the exact code the kernels run
+// (move lists, per-ply policies, random streams) against the oracle without
+// a GPU.  Nothing in the product loads this library.
+#include "../gpu_ai_gb300/csrc/rules.cuh"
+
+#include <cstring>
+
+using namespace ga;
+
+static Board load(const uint32_t *p) { return Board{p[0], p[1], p[2], p[3]}; }
+
+extern "C" {
+
+int rh_genmoves_b16(const uint32_t *pos, uint32_t n, uint8_t *out, uint32_t max_moves,
+                    uint8_t *counts) {
+  int rc = 0;
+  for (uint32_t i = 0; i < n; i++) {
+    const Board b = load(pos + 4 * (size_t)i);
+    Side s;
+    make_side(b, s);
+    uint32_t k = 0;
+    int c = for_each_move(s, jumpers(s), [&](int from, int to, uint32_t, int jumps, uint32_t dirs) {
+      if (k < max_moves) {
+        uint32_t w[8];
+        pack_move(b, from, to, jumps, dirs, w);
+        std::memcpy(out + 32 * ((size_t)i * max_moves + k), w, 32);
+      }
+      k++;
+      return false;
+    });
+    if (c < 0 || k > max_moves) rc = -1;
+    counts[i] = (uint8_t)(k > 255 ? 255 : k);
+  }
+  return rc;
+}
+
+int rh_count_moves(const uint32_t *pos) {
+  const Board b = load(pos);
+  Side s;
+  make_side(b, s);
+  return count_moves(s, jumpers(s));
+}
+
+// One playout with the kernel's per-ply code; returns the outcome.
+int rh_playout(const uint32_t *pos, uint64_t seed, uint64_t id, int policy, uint32_t *plies,
+               uint32_t *draws) {
+  Board b = load(pos);
+  Stream rs;
+  rs.init(seed, id, 0);
+  uint32_t p = 0;
+  int outcome = 0;
+  for (;;) {
+    if (((b.meta >> 8) & 0xffu) >= (uint32_t)kDrawPlies) { outcome = 0; break; }
+    int n = policy == 1 ? ply<1>(b, rs) : (policy == 2 ? ply<2>(b, rs) : ply<0>(b, rs));
+    if (n == 0) { outcome = (b.meta & 1u) ? 1 : -1; break; }
+    if (n < 0) { outcome = -100; break; }
+    p++;
+  }
+  if (plies) *plies = p;
+  if (draws) *draws = rs.k;
+  return outcome;
+}
+
+void rh_random_positions(uint64_t seed, uint32_t n, uint32_t min_plies, uint32_t max_plies,
+                         uint32_t *out) {
+  for (uint32_t p = 0; p < n; p++) {
+    Stream rs;
+    rs.init(seed, p, 1);
+    Board b = {0x00000FFFu, 0xFFF00000u, 0u, 0u};
+    const uint32_t np = min_plies + mulhi_index(rs.next(), max_plies - min_plies + 1u);
+    for (uint32_t q = 0; q < np; q++) {
+      if (((b.meta >> 8) & 0xffu) >= (uint32_t)kDrawPlies) break;
+      if (ply_random(b, rs) <= 0) break;
+    }
+    out[4 * p] = b.p1; out[4 * p + 1] = b.p2; out[4 * p + 2] = b.kings; out[4 * p + 3] = b.meta;
+  }
+}
+
+}  // extern "C"

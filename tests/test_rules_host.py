@@ -1,0 +1,79 @@
+"""The device rules header compiled for the host agrees with the oracle.
+
+gpu_ai_gb300/csrc/rules.cuh is the code the kernels run; a g++ build of it
+(tests/rules_host.cpp) is checked here on the CPU: move lists, the per-ply
+code of every policy, and the seeded position generator."""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+import oracle_lib as L
+from golden_boards import crafted_boards, random_boards
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+SO = os.path.join(HERE, "_build", "librules_host.so")
+SRC = os.path.join(HERE, "rules_host.cpp")
+HDR = os.path.join(os.path.dirname(HERE), "gpu_ai_gb300", "csrc", "rules.cuh")
+
+u32p = ctypes.POINTER(ctypes.c_uint32)
+u8p = ctypes.POINTER(ctypes.c_uint8)
+
+
+@pytest.fixture(scope="module")
+def rh():
+    if not os.path.exists(SO) or max(os.path.getmtime(SRC), os.path.getmtime(HDR)) > os.path.getmtime(SO):
+        os.makedirs(os.path.dirname(SO), exist_ok=True)
+        subprocess.run(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-Wno-unknown-pragmas", "-o", SO, SRC],
+                       check=True)
+    lib = ctypes.CDLL(SO)
+    lib.rh_genmoves_b16.argtypes = [u32p, ctypes.c_uint32, u8p, ctypes.c_uint32, u8p]
+    lib.rh_playout.argtypes = [u32p, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int, u32p, u32p]
+    lib.rh_random_positions.argtypes = [ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, u32p]
+    return lib
+
+
+def rh_genmoves(lib, pos, max_moves=64):
+    pos = np.ascontiguousarray(pos, dtype=np.uint32)
+    out = np.zeros((len(pos), max_moves, 32), np.uint8)
+    c = np.zeros(len(pos), np.uint8)
+    rc = lib.rh_genmoves_b16(pos.ctypes.data_as(u32p), len(pos), out.ctypes.data_as(u8p), max_moves,
+                             c.ctypes.data_as(u8p))
+    assert rc == 0
+    return out, c
+
+
+def test_moves_match_golden(rh, golden_movegen):
+    boards, moves, counts = golden_movegen
+    got, c = rh_genmoves(rh, boards, moves.shape[1])
+    np.testing.assert_array_equal(c, counts)
+    np.testing.assert_array_equal(got, moves)
+
+
+def test_moves_match_oracle(rh):
+    pos = np.concatenate([L.random_positions(5, 60000, 0, 150), random_boards(np.random.default_rng(1), 40000),
+                          crafted_boards()])
+    a, ca = L.genmoves(pos, 64)
+    b, cb = rh_genmoves(rh, pos, 64)
+    np.testing.assert_array_equal(ca, cb)
+    np.testing.assert_array_equal(a, b)
+
+
+def test_random_positions_match_oracle(rh):
+    out = np.zeros((5000, 4), np.uint32)
+    rh.rh_random_positions(2016, 5000, 0, 60, out.ctypes.data_as(u32p))
+    np.testing.assert_array_equal(out, L.random_positions(2016, 5000, 0, 60))
+
+
+@pytest.mark.parametrize("policy", [0, 1, 2])
+def test_playouts_replay_on_oracle(rh, policy):
+    pos = np.concatenate([L.random_positions(8, 300, 0, 60), crafted_boards()])
+    for i in range(1200):
+        p = np.ascontiguousarray(pos[i % len(pos)])
+        pl = np.zeros(1, np.uint32)
+        dr = np.zeros(1, np.uint32)
+        o = rh.rh_playout(p.ctypes.data_as(u32p), 77, 1000 + i, policy, pl.ctypes.data_as(u32p),
+                          dr.ctypes.data_as(u32p))
+        assert (o, int(pl[0]), int(dr[0])) == L.replay_one(p, 77, 1000 + i, policy), (policy, i)
