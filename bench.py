@@ -48,7 +48,7 @@ WORKLOAD = {
 # Lane-instructions per ply of the playout kernel, frozen from the first
 # correct kernel's ncu capture (smsp__thread_inst_executed.sum / plies);
 # the algorithmic work unit of the integer-issue roofline.
-OPS_PER_PLY = 0.0
+OPS_PER_PLY = 260.0
 # DRAM bytes per launch of the playout kernel from one ncu capture
 # (dram__bytes_read.sum + dram__bytes_write.sum); None until captured.
 TRAFFIC_BYTES = None
@@ -212,13 +212,16 @@ def run_ours(args):
 
     torch.cuda.set_device(local)
     eng = Engine(local)
+    if args.block:
+        eng.set_launch(0, args.block, args.blocks_per_sm)
     info = eng.device_info()
     positions = eng.random_positions(POS_SEED, N_POS, 0, MAX_PLIES)
     reps = np.full(N_POS, REPS, dtype=np.uint32)
     d_pos = torch.from_numpy(positions.view(np.int32).copy()).cuda()
     d_out = torch.empty(TOTAL, dtype=torch.int8, device="cuda")
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
-    stream = torch.cuda.current_stream()
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     sid = stream.cuda_stream
     base = (rank << 40)
 
@@ -320,6 +323,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--block", type=int, default=0, help="threads per block of the playout kernel (0: default)")
+    ap.add_argument("--blocks-per-sm", type=int, default=0, help="resident blocks per SM (0: as many as fit)")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")

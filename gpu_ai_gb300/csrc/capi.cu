@@ -96,7 +96,9 @@ struct gpuai_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
   int sms = 0;
-  int blocks_per_sm[3] = {0, 0, 0};
+  int block[3] = {ga::kPlayoutBlock, ga::kPlayoutBlock, ga::kPlayoutBlock};
+  int blocks_per_sm[3] = {0, 0, 0};  // resident blocks per SM used for the grid
+  int max_blocks_per_sm[3] = {0, 0, 0};
   Control *ctl = nullptr;  // device
   DevBuf d_in, d_off, d_out, d_aux;
   HostBuf h_in, h_out;
@@ -122,7 +124,7 @@ int set_device(gpuai_ctx *ctx) {
 
 int grid_for(gpuai_ctx *ctx, int policy, uint32_t total) {
   long long resident = (long long)ctx->sms * ctx->blocks_per_sm[policy];
-  long long need = ((long long)total + ga::kPlayoutBlock - 1) / ga::kPlayoutBlock;
+  long long need = ((long long)total + ctx->block[policy] - 1) / ctx->block[policy];
   long long g = need < resident ? need : resident;
   return (int)(g < 1 ? 1 : g);
 }
@@ -144,7 +146,7 @@ int launch_device(gpuai_ctx *ctx, const gpuai_board *d_pos, const uint32_t *d_of
   a.counter = &ctx->ctl->counter;
   a.status = &ctx->ctl->status;
   a.plies = &ctx->ctl->plies;
-  CK(ga::launch_playouts(a, policy, grid_for(ctx, policy, total), s), "playout kernel launch");
+  CK(ga::launch_playouts(a, policy, ctx->block[policy], grid_for(ctx, policy, total), s), "playout kernel launch");
   return GPUAI_OK;
 }
 
@@ -175,9 +177,10 @@ int gpuai_create(int device, gpuai_ctx **out) {
     else ctx->sms = prop.multiProcessorCount;
   }
   for (int p = 0; rc == GPUAI_OK && p < 3; p++) {
-    e = ga::playout_occupancy(p, &ctx->blocks_per_sm[p]);
+    e = ga::playout_occupancy(p, ctx->block[p], &ctx->max_blocks_per_sm[p]);
     if (e != cudaSuccess) rc = cuda_fail(e, "occupancy query");
-    else if (ctx->blocks_per_sm[p] < 1) ctx->blocks_per_sm[p] = 1;
+    else if (ctx->max_blocks_per_sm[p] < 1) ctx->max_blocks_per_sm[p] = 1;
+    ctx->blocks_per_sm[p] = ctx->max_blocks_per_sm[p];
   }
   if (rc == GPUAI_OK) {
     e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
@@ -214,7 +217,35 @@ int gpuai_device_info(gpuai_ctx *ctx, int32_t *sms, int32_t *blocks_per_sm, int3
   if (!ctx) return fail(GPUAI_ERR_INVALID, "gpuai_device_info: ctx is NULL");
   if (sms) *sms = ctx->sms;
   if (blocks_per_sm) *blocks_per_sm = ctx->blocks_per_sm[0];
-  if (block_threads) *block_threads = ga::kPlayoutBlock;
+  if (block_threads) *block_threads = ctx->block[0];
+  return GPUAI_OK;
+}
+
+int gpuai_set_launch(gpuai_ctx *ctx, int32_t policy, int32_t block_threads, int32_t blocks_per_sm) {
+  if (!ctx) return fail(GPUAI_ERR_INVALID, "gpuai_set_launch: ctx is NULL");
+  if (policy < 0 || policy > 2) return fail(GPUAI_ERR_INVALID, "gpuai_set_launch: unknown policy %d", policy);
+  if (!ga::valid_block(block_threads))
+    return fail(GPUAI_ERR_INVALID, "gpuai_set_launch: block_threads %d not in {64,128,256,512}", block_threads);
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  int rc = set_device(ctx);
+  if (rc) return rc;
+  int maxb = 0;
+  CK(ga::playout_occupancy(policy, block_threads, &maxb), "occupancy query");
+  if (maxb < 1) return fail(GPUAI_ERR_INVALID, "gpuai_set_launch: block of %d threads cannot be resident", block_threads);
+  if (blocks_per_sm < 0) return fail(GPUAI_ERR_INVALID, "gpuai_set_launch: negative blocks_per_sm");
+  ctx->block[policy] = block_threads;
+  ctx->max_blocks_per_sm[policy] = maxb;
+  ctx->blocks_per_sm[policy] = (blocks_per_sm == 0 || blocks_per_sm > maxb) ? maxb : blocks_per_sm;
+  return GPUAI_OK;
+}
+
+int gpuai_get_launch(gpuai_ctx *ctx, int32_t policy, int32_t *block_threads, int32_t *blocks_per_sm,
+                     int32_t *max_blocks_per_sm) {
+  if (!ctx) return fail(GPUAI_ERR_INVALID, "gpuai_get_launch: ctx is NULL");
+  if (policy < 0 || policy > 2) return fail(GPUAI_ERR_INVALID, "gpuai_get_launch: unknown policy %d", policy);
+  if (block_threads) *block_threads = ctx->block[policy];
+  if (blocks_per_sm) *blocks_per_sm = ctx->blocks_per_sm[policy];
+  if (max_blocks_per_sm) *max_blocks_per_sm = ctx->max_blocks_per_sm[policy];
   return GPUAI_OK;
 }
 
@@ -283,7 +314,7 @@ int gpuai_playouts_device(gpuai_ctx *ctx, const gpuai_board *d_pos, const uint32
   std::lock_guard<std::mutex> lock(ctx->mu);
   int rc = set_device(ctx);
   if (rc) return rc;
-  cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);  // NULL: the legacy default stream
   return launch_device(ctx, d_pos, d_offsets, npos, uniform_reps, total, seed, stream_base, policy,
                        d_out, s);
 }

@@ -33,66 +33,126 @@ __device__ __forceinline__ Board load_board(const Board *p) {
 
 // ---- the playout kernel
 
-template <int POLICY>
-__global__ void __launch_bounds__(kPlayoutBlock) playout_kernel(PlayoutArgs a) {
+// Lanes without a game take the next playout indices: one atomicAdd per warp.
+// Returns true for lanes that got a playout (index in j).
+__device__ __forceinline__ bool claim(const PlayoutArgs &a, bool have, uint32_t &j, bool &exhausted,
+                                      uint32_t lane) {
+  const uint32_t need = __ballot_sync(kFull, !have);
+  if (!need || exhausted) return false;
+  const uint32_t cnt = __popc(need);
+  const uint32_t leader = __ffs(need) - 1;
+  uint32_t base = 0;
+  if (lane == leader) base = atomicAdd(a.counter, cnt);
+  base = __shfl_sync(kFull, base, leader);
+  if (base + cnt >= a.total) exhausted = true;
+  if (have) return false;
+  j = base + __popc(need & ((1u << lane) - 1u));
+  return j < a.total;
+}
+
+// Play one ply of the lane's game; returns true when the game is over and
+// sets the outcome (+1 / -1 / 0).
+template <int POLICY, class Rng>
+__device__ __forceinline__ bool step_game(const PlayoutArgs &a, Board &b, Rng &rs, uint32_t &game_plies,
+                                          uint32_t &plies_here, int &outcome) {
+  outcome = 0;
+  if (((b.meta >> 8) & 0xffu) >= (uint32_t)kDrawPlies) return true;
+  const int n = ply<POLICY>(b, rs);
+  if (n == 0) {
+    outcome = (b.meta & 1u) ? 1 : -1;  // side to move cannot move and loses
+    return true;
+  }
+  if (n < 0) {
+    atomicOr(a.status, kStatusDepth);
+    return true;
+  }
+  if (++game_plies > kMaxPlies) {
+    atomicOr(a.status, kStatusPlyCap);
+    return true;
+  }
+  plies_here++;
+  return false;
+}
+
+template <int POLICY, int BLOCK>
+__global__ void __launch_bounds__(BLOCK) playout_kernel(PlayoutArgs a) {
   const uint32_t lane = threadIdx.x & 31u;
-  const uint32_t lt_mask = (1u << lane) - 1u;
   Board b = {0, 0, 0, 0};
-  Stream rs;
-  rs.init(0, 0, 0);
   uint32_t j = 0, plies_here = 0, game_plies = 0;
   bool have = false, exhausted = false;
-  unsigned long long my_plies = 0;
 
-  for (;;) {
-    // lanes without a game take the next playout indices (one atomic per warp)
-    const uint32_t need = __ballot_sync(kFull, !have);
-    if (need && !exhausted) {
-      const uint32_t cnt = __popc(need);
-      const uint32_t leader = __ffs(need) - 1;
-      uint32_t base = 0;
-      if (lane == leader) base = atomicAdd(a.counter, cnt);
-      base = __shfl_sync(kFull, base, leader);
-      if (base + cnt >= a.total) exhausted = true;
-      if (!have) {
-        j = base + __popc(need & lt_mask);
-        if (j < a.total) {
+  if constexpr (POLICY == 0) {
+    // Uniform random policy: at most one draw per ply, so Philox blocks are
+    // generated for the whole warp every fourth iteration (DrawRing keeps four
+    // or more draws buffered) and new games start on those iterations too.
+    // Plies whose capture can be extended (about 3% of plies) are deferred to
+    // every kSearchPeriod-th iteration, so that the lanes needing the longer
+    // capture code run it together and the per-iteration code stays
+    // branch-free for the others.
+    DrawRing rs;
+    rs.start(0, 0, 0);
+    bool pending = false;
+    auto pick = [&](uint32_t n) { return rs.pick(n); };
+    for (uint32_t it = 0;; ++it) {
+      if ((it & 3u) == 0) {
+        if (claim(a, have, j, exhausted, lane)) {
           have = true;
           b = load_board(a.pos + position_of(a, j));
-          rs.init(a.seed, a.stream_base + j, 0);
+          rs.start(a.seed, a.stream_base + j, 0);
           game_plies = 0;
         }
+        if (!__any_sync(kFull, have)) break;
+        if (have) rs.refill();
       }
-    }
-    if (!__any_sync(kFull, have)) break;
-    if (have) {
-      int outcome = 0;
-      bool fin = false;
-      if (((b.meta >> 8) & 0xffu) >= (uint32_t)kDrawPlies) {
-        fin = true;
+      if (!have) continue;
+      int n;
+      if (pending) {
+        if ((it & (kSearchPeriod - 1u)) != 0) continue;
+        pending = false;
+        n = play_ply_fast<false>(b, pick);
       } else {
-        const int n = ply<POLICY>(b, rs);
-        if (n == 0) {
-          fin = true;
-          outcome = (b.meta & 1u) ? 1 : -1;  // side to move cannot move and loses
-        } else if (n < 0) {
-          fin = true;
-          atomicOr(a.status, kStatusDepth);
-        } else if (++game_plies > kMaxPlies) {
-          fin = true;
-          atomicOr(a.status, kStatusPlyCap);
-        } else {
-          plies_here++;
+        if (((b.meta >> 8) & 0xffu) >= (uint32_t)kDrawPlies) {
+          a.out[j] = 0;
+          have = false;
+          continue;
+        }
+        n = play_ply_fast<true>(b, pick);
+        if (n == kNeedSearch) {
+          pending = true;
+          continue;
         }
       }
-      if (fin) {
-        a.out[j] = (int8_t)outcome;
-        have = false;
+      if (n > 0 && ++game_plies <= kMaxPlies) {
+        plies_here++;
+        continue;
+      }
+      if (n < 0) atomicOr(a.status, kStatusDepth);
+      else if (n > 0) atomicOr(a.status, kStatusPlyCap);
+      a.out[j] = (int8_t)(n == 0 ? ((b.meta & 1u) ? 1 : -1) : 0);  // side to move cannot move: loses
+      have = false;
+    }
+  } else {
+    Stream rs;
+    rs.init(0, 0, 0);
+    for (;;) {
+      if (claim(a, have, j, exhausted, lane)) {
+        have = true;
+        b = load_board(a.pos + position_of(a, j));
+        rs.init(a.seed, a.stream_base + j, 0);
+        game_plies = 0;
+      }
+      if (!__any_sync(kFull, have)) break;
+      if (have) {
+        int outcome;
+        if (step_game<POLICY>(a, b, rs, game_plies, plies_here, outcome)) {
+          a.out[j] = (int8_t)outcome;
+          have = false;
+        }
       }
     }
   }
   if (a.plies != nullptr) {
-    my_plies = plies_here;
+    unsigned long long my_plies = plies_here;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) my_plies += __shfl_xor_sync(kFull, my_plies, o);
     if (lane == 0) atomicAdd(a.plies, my_plies);
@@ -147,19 +207,31 @@ __global__ void random_positions_kernel(uint64_t seed, uint32_t n, uint32_t min_
 
 // ---- launchers
 
-cudaError_t playout_occupancy(int policy, int *blocks_per_sm) {
-  if (policy == 1)
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, playout_kernel<1>, kPlayoutBlock, 0);
-  if (policy == 2)
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, playout_kernel<2>, kPlayoutBlock, 0);
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, playout_kernel<0>, kPlayoutBlock, 0);
+template <int POLICY>
+static const void *kernel_for(int block) {
+  switch (block) {
+    case 64: return (const void *)playout_kernel<POLICY, 64>;
+    case 128: return (const void *)playout_kernel<POLICY, 128>;
+    case 512: return (const void *)playout_kernel<POLICY, 512>;
+    default: return (const void *)playout_kernel<POLICY, 256>;
+  }
 }
 
-cudaError_t launch_playouts(const PlayoutArgs &a, int policy, int grid, cudaStream_t s) {
-  if (policy == 1) playout_kernel<1><<<grid, kPlayoutBlock, 0, s>>>(a);
-  else if (policy == 2) playout_kernel<2><<<grid, kPlayoutBlock, 0, s>>>(a);
-  else playout_kernel<0><<<grid, kPlayoutBlock, 0, s>>>(a);
-  return cudaGetLastError();
+static const void *playout_fn(int policy, int block) {
+  if (policy == 1) return kernel_for<1>(block);
+  if (policy == 2) return kernel_for<2>(block);
+  return kernel_for<0>(block);
+}
+
+bool valid_block(int block) { return block == 64 || block == 128 || block == 256 || block == 512; }
+
+cudaError_t playout_occupancy(int policy, int block, int *blocks_per_sm) {
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, playout_fn(policy, block), block, 0);
+}
+
+cudaError_t launch_playouts(const PlayoutArgs &a, int policy, int block, int grid, cudaStream_t s) {
+  void *args[] = {const_cast<PlayoutArgs *>(&a)};
+  return cudaLaunchKernel(playout_fn(policy, block), dim3(grid), dim3(block), args, 0, s);
 }
 
 cudaError_t launch_genmoves(const Board *pos, uint32_t n, void *out, uint32_t max_moves,

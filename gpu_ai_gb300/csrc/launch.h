@@ -13,8 +13,9 @@ constexpr uint32_t kStatusDepth = 1u;     // capture sequence deeper than kMaxDe
 constexpr uint32_t kStatusOverflow = 2u;  // move list longer than the caller's buffer
 constexpr uint32_t kStatusPlyCap = 4u;    // playout exceeded kMaxPlies (cannot happen under the 50-ply rule)
 
-constexpr int kPlayoutBlock = 256;
+constexpr int kPlayoutBlock = 256;        // default threads per block
 constexpr uint32_t kMaxPlies = 4096;
+constexpr uint32_t kSearchPeriod = 8;     // iterations between deferred capture searches (power of 2, >= 4)
 
 struct PlayoutArgs {
   const Board *pos;
@@ -30,9 +31,11 @@ struct PlayoutArgs {
   unsigned long long *plies;      // plies played (optional)
 };
 
-// Resident blocks per SM of the playout kernel for `policy`.
-cudaError_t playout_occupancy(int policy, int *blocks_per_sm);
-cudaError_t launch_playouts(const PlayoutArgs &a, int policy, int grid, cudaStream_t s);
+// Playout kernels are instantiated for blocks of 64, 128, 256 and 512 threads.
+bool valid_block(int block);
+// Resident blocks per SM of the playout kernel for `policy` and `block`.
+cudaError_t playout_occupancy(int policy, int block, int *blocks_per_sm);
+cudaError_t launch_playouts(const PlayoutArgs &a, int policy, int block, int grid, cudaStream_t s);
 cudaError_t launch_genmoves(const Board *pos, uint32_t n, void *out, uint32_t max_moves,
                             uint8_t *counts, uint32_t *status, cudaStream_t s);
 cudaError_t launch_random_positions(uint64_t seed, uint32_t n, uint32_t min_plies,

@@ -68,13 +68,12 @@ GA_HD uint32_t step(uint32_t b) {
 }
 
 // Square offset of a jump (two steps) in direction d: +9, +7, -7, -9.
-GA_HD int jump_off(int d) { return d == 0 ? 9 : (d == 1 ? 7 : (d == 2 ? -7 : -9)); }
+GA_HD int jump_off(int d) { return (int)((0x00021012u >> (8 * d)) & 0xffu) - 9; }
 
 // Square offset of a single step from square s in direction d.
 GA_HD int step_off(int s, int d) {
-  int even = ((s >> 2) & 1) ^ 1;  // row parity of s
-  int base = d == 0 ? 4 : (d == 1 ? 3 : (d == 2 ? -4 : -5));
-  return base + even;
+  const int even = ((s >> 2) & 1) ^ 1;  // row parity of s
+  return (int)((0x00010809u >> (8 * d)) & 0xffu) - 5 + even;  // 4, 3, -4, -5 on odd rows
 }
 
 // Square jumped over when moving from a to b = a + jump_off(d).
@@ -90,6 +89,30 @@ struct Side {
   uint32_t jd[4];  // squares from which a jump in direction d is possible
 };
 
+// Jump sources per direction (both the jumped and the landing square on the
+// board); a jump moves the square index by +9, +7, -7, -9 for D0..D3.
+constexpr uint32_t kJumpSrc0 = 0x00777777u, kJumpSrc1 = 0x00EEEEEEu;
+constexpr uint32_t kJumpSrc2 = 0x77777700u, kJumpSrc3 = 0xEEEEEE00u;
+
+// Landing squares of jumps in direction D from the squares of x (x must be
+// valid jump sources for D).
+template <int D>
+GA_HD uint32_t jump2(uint32_t x) {
+  if (D == 0) return x << 9;
+  if (D == 1) return x << 7;
+  if (D == 2) return x >> 7;
+  return x >> 9;
+}
+
+// Squares s with s + jump(D) in x and s a valid jump source.
+template <int D>
+GA_HD uint32_t jump2_back(uint32_t x) {
+  if (D == 0) return (x >> 9) & kJumpSrc0;
+  if (D == 1) return (x >> 7) & kJumpSrc1;
+  if (D == 2) return (x << 7) & kJumpSrc2;
+  return (x << 9) & kJumpSrc3;
+}
+
 GA_HD void make_side(const Board &b, Side &s) {
   s.turn = (int)(b.meta & 1u);
   s.own = s.turn ? b.p2 : b.p1;
@@ -97,10 +120,10 @@ GA_HD void make_side(const Board &b, Side &s) {
   s.ownK = s.own & b.kings;
   s.empty = ~(b.p1 | b.p2);
   // jd[d] = {s : s+d is an opponent, s+2d is empty}; step<3-d> is the inverse of step<d>.
-  s.jd[0] = step<3>(s.opp) & step<3>(step<3>(s.empty));
-  s.jd[1] = step<2>(s.opp) & step<2>(step<2>(s.empty));
-  s.jd[2] = step<1>(s.opp) & step<1>(step<1>(s.empty));
-  s.jd[3] = step<0>(s.opp) & step<0>(step<0>(s.empty));
+  s.jd[0] = step<3>(s.opp) & jump2_back<0>(s.empty);
+  s.jd[1] = step<2>(s.opp) & jump2_back<1>(s.empty);
+  s.jd[2] = step<1>(s.opp) & jump2_back<2>(s.empty);
+  s.jd[3] = step<0>(s.opp) & jump2_back<3>(s.empty);
 }
 
 // Pieces of the side to move that have at least one capture.
@@ -388,74 +411,327 @@ GA_HD int eps_delta(const Board &b, const Side &s, int from, int to, uint32_t re
 
 // ------------------------------------------------------------ one random ply
 
-// Outcome of a finished game from the side to move's view is computed by the
-// caller; this returns the number of legal moves and applies move
-// index(n) for n >= 1.  `pick` maps n (>= 2) to an index in [0, n).
-// Returns -1 on an internal limit (capture deeper than kMaxDepth).
+// Position of the rem-th set bit (ascending) of a 4-bit mask dm.
+GA_HD int nth_bit4(uint32_t dm, uint32_t rem) {
+  const uint32_t idx = dm * 4u + rem;  // 0..63, 2-bit entries, 16 per word
+  const uint32_t w = idx >> 4;
+  const uint32_t word = w == 0 ? 0x04010000u : (w == 1 ? 0x24090802u : (w == 2 ? 0x340D0C03u : 0xE439380Eu));
+  return (int)((word >> (2u * (idx & 15u))) & 3u);
+}
+
+// Squares of the side to move whose capture can continue after the first
+// jump (they need the depth-first search); J[d] are the first-jump sources.
+GA_HD uint32_t continuing_sources(const Side &s, const uint32_t J[4]) {
+  const uint32_t men = s.own & ~s.ownK;
+  const uint32_t jall = s.jd[0] | s.jd[1] | s.jd[2] | s.jd[3];
+  const uint32_t jf = s.turn ? (s.jd[2] | s.jd[3]) : (s.jd[0] | s.jd[1]);
+  const uint32_t cm = (J[0] & jump2_back<0>(jf)) | (J[1] & jump2_back<1>(jf)) | (J[2] & jump2_back<2>(jf)) |
+                      (J[3] & jump2_back<3>(jf));
+  const uint32_t ck = (J[0] & jump2_back<0>(jall)) | (J[1] & jump2_back<1>(jall)) |
+                      (J[2] & jump2_back<2>(jall)) | (J[3] & jump2_back<3>(jall));
+  return (cm & men) | (ck & s.ownK);
+}
+
+// General ply: returns the number of legal moves and applies move
+// pick(n) for n >= 1, where `pick` maps n to an index in [0, n), drawing from
+// the random stream only when n >= 2.
+// Captures whose first jump can be extended are enumerated by the
+// depth-first search (counts of the first four such squares are kept, so each
+// is walked once to count and at most once more to select); single jumps are
+// counted from the direction masks.  Returns -1 on an internal limit (capture
+// deeper than kMaxDepth).
 template <class Pick>
 GA_HD int play_ply(Board &b, Pick &&pick) {
   Side s;
   make_side(b, s);
-  uint32_t J = jumpers(s);
-  if (J) {
-    // count all capture sequences, squares ascending
-    int n = 0;
-    for (uint32_t m = J; m; m &= m - 1) {
-      int c = capture_walk(s, ctz(m), [](int, uint32_t, int, uint32_t) { return false; });
+  const uint32_t m01 = s.turn ? s.ownK : s.own;
+  const uint32_t m23 = s.turn ? s.own : s.ownK;
+  const uint32_t J[4] = {m01 & s.jd[0], m01 & s.jd[1], m23 & s.jd[2], m23 & s.jd[3]};
+  const uint32_t Jall = J[0] | J[1] | J[2] | J[3];
+  if (Jall) {
+    const uint32_t men = s.own & ~s.ownK;
+    const uint32_t X = continuing_sources(s, J);
+    int n = popc(J[0] & ~X) + popc(J[1] & ~X) + popc(J[2] & ~X) + popc(J[3] & ~X);
+    uint32_t cache = 0;  // 8-bit sequence counts of the first four searched squares
+    int q = 0;
+    for (uint32_t m = X; m; m &= m - 1) {
+      const int c = capture_walk(s, ctz(m), [](int, uint32_t, int, uint32_t) { return false; });
       if (c < 0) return -1;
       n += c;
+      if (q < 4) cache |= (uint32_t)(c < 255 ? c : 255) << (8 * q++);
     }
-    uint32_t i = n >= 2 ? pick((uint32_t)n) : 0u;
-    for (uint32_t m = J; m; m &= m - 1) {
-      int o = ctz(m);
-      int to = -1;
-      uint32_t rem_mask = 0;
-      uint32_t want = i;
-      int c = capture_walk(s, o, [&](int t, uint32_t removed, int, uint32_t) {
-        if (want == 0) { to = t; rem_mask = removed; return true; }
-        want--;
-        return false;
-      });
-      if (to >= 0) { apply_move(b, o, to, rem_mask); return n; }
-      i -= (uint32_t)c;
+    uint32_t i = pick((uint32_t)n);
+    q = 0;
+    for (uint32_t m = Jall; m; m &= m - 1) {
+      const int sq = ctz(m);
+      if ((X >> sq) & 1u) {
+        uint32_t c = q < 4 ? (cache >> (8 * q)) & 0xffu : 255u;
+        if (c == 255u) c = (uint32_t)capture_walk(s, sq, [](int, uint32_t, int, uint32_t) { return false; });
+        q++;
+        if (i >= c) {
+          i -= c;
+          continue;
+        }
+        int to = -1;
+        uint32_t rem_mask = 0, want = i;
+        capture_walk(s, sq, [&](int t, uint32_t removed, int, uint32_t) {
+          if (want == 0) { to = t; rem_mask = removed; return true; }
+          want--;
+          return false;
+        });
+        apply_move(b, sq, to, rem_mask);
+        return n;
+      }
+      const uint32_t dm = ((J[0] >> sq) & 1u) | (((J[1] >> sq) & 1u) << 1) | (((J[2] >> sq) & 1u) << 2) |
+                          (((J[3] >> sq) & 1u) << 3);
+      const uint32_t cnt = (uint32_t)popc(dm);
+      if (i >= cnt) {
+        i -= cnt;
+        continue;
+      }
+      // men search dc = -1 first: the reverse of the ascending direction order
+      const uint32_t rem = ((men >> sq) & 1u) ? cnt - 1u - i : i;
+      const int d = nth_bit4(dm, rem);
+      const int to = sq + jump_off(d);
+      apply_move(b, sq, to, 1u << mid_square(sq, to));
+      return n;
     }
-    return -1;  // unreachable
+    return -1;  // unreachable: i < n
   }
   uint32_t md[4];
   direct_masks(s, md);
-  int n = popc(md[0]) + popc(md[1]) + popc(md[2]) + popc(md[3]);
+  const int n = popc(md[0]) + popc(md[1]) + popc(md[2]) + popc(md[3]);
   if (n == 0) return 0;
-  uint32_t i = n >= 2 ? pick((uint32_t)n) : 0u;
-  uint32_t any = md[0] | md[1] | md[2] | md[3];
-  for (;;) {
-    int sq = ctz(any);
-    uint32_t c0 = (md[0] >> sq) & 1u, c1 = (md[1] >> sq) & 1u, c2 = (md[2] >> sq) & 1u,
-             c3 = (md[3] >> sq) & 1u;
-    uint32_t c = c0 + c1 + c2 + c3;
+  uint32_t i = pick((uint32_t)n);
+  for (uint32_t any = md[0] | md[1] | md[2] | md[3];; any &= any - 1) {
+    const int sq = ctz(any);
+    const uint32_t dm = ((md[0] >> sq) & 1u) | (((md[1] >> sq) & 1u) << 1) | (((md[2] >> sq) & 1u) << 2) |
+                        (((md[3] >> sq) & 1u) << 3);
+    const uint32_t c = (uint32_t)popc(dm);
     if (i < c) {
-      // i-th set direction at sq, ascending
-      int d;
-      uint32_t dm = c0 | (c1 << 1) | (c2 << 2) | (c3 << 3);
-      for (uint32_t q = 0; q < i; q++) dm &= dm - 1;
-      d = ctz(dm);
+      const int d = nth_bit4(dm, i);
       apply_move(b, sq, sq + step_off(sq, d), 0u);
       return n;
     }
     i -= c;
-    any &= any - 1;
   }
 }
+
+// ------------------------------------------------------------ men's multi-jumps
+
+// Number of maximal capture continuations C(t) in 1..4 for a man of the side
+// to move that has just landed on square t, for every square at once, as
+// three bit-planes.  Men only move forward, so C(t) depends on the original
+// board alone (captured pieces stay on the board during the search, and no
+// square is visited twice): C(t) = 1 without a further jump, else the sum of
+// C over the landing squares of the possible jumps.  FA/FB are the forward
+// directions in search order (dc = -1 first).  Two rounds are exact for every
+// square a first jump can land on.
+struct ManTree {
+  uint32_t c0, c1, c2;
+  GA_HD uint32_t at(int t) const {
+    return ((c0 >> t) & 1u) + 2u * ((c1 >> t) & 1u) + 4u * ((c2 >> t) & 1u);
+  }
+};
+
+template <int FA, int FB>
+GA_HD ManTree man_tree(const Side &s) {
+  const uint32_t A = s.jd[FA], B = s.jd[FB], any = A | B;
+  uint32_t c0 = ~0u, c1 = 0u, c2 = 0u;
+#pragma unroll
+  for (int r = 0; r < 2; r++) {
+    const uint32_t a0 = jump2_back<FA>(c0) & A, a1 = jump2_back<FA>(c1) & A, a2 = jump2_back<FA>(c2) & A;
+    const uint32_t b0 = jump2_back<FB>(c0) & B, b1 = jump2_back<FB>(c1) & B, b2 = jump2_back<FB>(c2) & B;
+    const uint32_t s0 = a0 ^ b0, k0 = a0 & b0;
+    const uint32_t s1 = a1 ^ b1 ^ k0, k1 = (a1 & b1) | (k0 & (a1 ^ b1));
+    const uint32_t s2 = a2 ^ b2 ^ k1;
+    c0 = s0 | ~any;
+    c1 = s1 & any;
+    c2 = s2 & any;
+  }
+  return ManTree{c0, c1, c2};
+}
+
+// Number of capture sequences a man on each square of m starts with a jump in
+// direction F, weighted by the continuations C of its landing square.
+template <int F>
+GA_HD int man_weight(uint32_t m, const ManTree &c) {
+  return popc(m & jump2_back<F>(c.c0)) + 2 * popc(m & jump2_back<F>(c.c1)) + 4 * popc(m & jump2_back<F>(c.c2));
+}
+
+// A capture ply where some man can continue a capture but no king can: the
+// move list is counted with man_tree instead of a search and move i is found
+// by descending it.
+template <int FA, int FB, class Pick>
+GA_HD int play_ply_men_multi(Board &b, const Side &s, const uint32_t J[4], Pick &&pick) {
+  const uint32_t men = s.own & ~s.ownK;
+  const ManTree c = man_tree<FA, FB>(s);
+  const uint32_t mA = J[FA] & men, mB = J[FB] & men;
+  const uint32_t k0 = J[0] & s.ownK, k1 = J[1] & s.ownK, k2 = J[2] & s.ownK, k3 = J[3] & s.ownK;
+  const int n = man_weight<FA>(mA, c) + man_weight<FB>(mB, c) + popc(k0) + popc(k1) + popc(k2) + popc(k3);
+  uint32_t i = pick((uint32_t)n);
+  for (uint32_t X = J[0] | J[1] | J[2] | J[3]; X; X &= X - 1) {
+    const int sq = ctz(X);
+    if ((men >> sq) & 1u) {
+      const uint32_t wa = ((mA >> sq) & 1u) ? c.at(sq + jump_off(FA)) : 0u;
+      const uint32_t wb = ((mB >> sq) & 1u) ? c.at(sq + jump_off(FB)) : 0u;
+      if (i >= wa + wb) {
+        i -= wa + wb;
+        continue;
+      }
+      // descend: at each landing take the first direction whose subtree holds i
+      int t = sq;
+      uint32_t removed = 0;
+      uint32_t availA = (mA >> sq) & 1u, availB = (mB >> sq) & 1u;
+      while (availA | availB) {
+        const uint32_t w = availA ? c.at(t + jump_off(FA)) : 0u;
+        const int f = (availA && i < w) ? FA : FB;
+        if (f == FB) i -= w;
+        const int nt = t + jump_off(f);
+        removed |= 1u << mid_square(t, nt);
+        t = nt;
+        availA = (s.jd[FA] >> t) & 1u;
+        availB = (s.jd[FB] >> t) & 1u;
+      }
+      apply_move(b, sq, t, removed);
+      return n;
+    }
+    const uint32_t dm = ((k0 >> sq) & 1u) | (((k1 >> sq) & 1u) << 1) | (((k2 >> sq) & 1u) << 2) |
+                        (((k3 >> sq) & 1u) << 3);
+    const uint32_t cnt = (uint32_t)popc(dm);
+    if (i >= cnt) {
+      i -= cnt;
+      continue;
+    }
+    const int d = nth_bit4(dm, i);
+    const int to = sq + jump_off(d);
+    apply_move(b, sq, to, 1u << mid_square(sq, to));
+    return n;
+  }
+  return -1;  // unreachable: i < n
+}
+
+constexpr int kNeedSearch = -2;
+
+// One uniformly random ply, branch-free for direct moves and for captures
+// that cannot be extended (the common cases).  Positions where some capture
+// can continue take the bit-sliced men's tree (play_ply_men_multi) or the
+// depth-first search (play_ply); with DEFER they instead return kNeedSearch
+// without touching the board or the stream, and the caller runs
+// play_ply_fast<false> later.  Same move list order, same index -> move map as
+// play_ply.
+template <bool DEFER = false, class Pick>
+GA_HD int play_ply_fast(Board &b, Pick &&pick) {
+  Side s;
+  make_side(b, s);
+  const uint32_t men = s.own & ~s.ownK;
+  const uint32_t m01 = s.turn ? s.ownK : s.own;  // D0/D1 movers: P1 men and all kings
+  const uint32_t m23 = s.turn ? s.own : s.ownK;  // D2/D3 movers: P2 men and all kings
+  const uint32_t J0 = m01 & s.jd[0], J1 = m01 & s.jd[1], J2 = m23 & s.jd[2], J3 = m23 & s.jd[3];
+  const bool capture = (J0 | J1 | J2 | J3) != 0;
+  // landing squares from which the same piece could jump again
+  const uint32_t jall = s.jd[0] | s.jd[1] | s.jd[2] | s.jd[3];
+  const uint32_t jf = s.turn ? (s.jd[2] | s.jd[3]) : (s.jd[0] | s.jd[1]);
+  const uint32_t lm = jump2<0>(J0 & men) | jump2<1>(J1 & men) | jump2<2>(J2 & men) | jump2<3>(J3 & men);
+  const uint32_t lk = jump2<0>(J0 & s.ownK) | jump2<1>(J1 & s.ownK) | jump2<2>(J2 & s.ownK) |
+                      jump2<3>(J3 & s.ownK);
+  const uint32_t cont_k = lk & jall, cont_m = lm & jf;
+  if (cont_k | cont_m) {
+    if (DEFER) return kNeedSearch;
+    if (cont_k) return play_ply(b, pick);  // a king can continue: depth-first search with the cycle check
+    // only men continue: counted on the bit-sliced continuation tree
+    const uint32_t J[4] = {J0, J1, J2, J3};
+    return s.turn ? play_ply_men_multi<3, 2>(b, s, J, pick) : play_ply_men_multi<1, 0>(b, s, J, pick);
+  }
+  const uint32_t M0 = capture ? J0 : (m01 & step<3>(s.empty));
+  const uint32_t M1 = capture ? J1 : (m01 & step<2>(s.empty));
+  const uint32_t M2 = capture ? J2 : (m23 & step<1>(s.empty));
+  const uint32_t M3 = capture ? J3 : (m23 & step<0>(s.empty));
+  const int n = popc(M0) + popc(M1) + popc(M2) + popc(M3);
+  if (n == 0) return 0;
+  const uint32_t i = pick((uint32_t)n);
+  // square of move i: the largest x with (moves from squares < x) <= i
+  uint32_t lo = 0, clo = 0;
+#pragma unroll
+  for (uint32_t st = 16; st >= 1; st >>= 1) {
+    const uint32_t mid = lo + st;
+    const uint32_t L = (1u << mid) - 1u;
+    const uint32_t c = (uint32_t)(popc(M0 & L) + popc(M1 & L) + popc(M2 & L) + popc(M3 & L));
+    const bool le = c <= i;
+    lo = le ? mid : lo;
+    clo = le ? c : clo;
+  }
+  const int sq = (int)lo;
+  const uint32_t rem = i - clo;
+  const uint32_t dm = ((M0 >> sq) & 1u) | (((M1 >> sq) & 1u) << 1) | (((M2 >> sq) & 1u) << 2) |
+                      (((M3 >> sq) & 1u) << 3);
+  // men search captures dc=-1 first: the reverse of the ascending direction order
+  const bool reverse = capture && ((men >> sq) & 1u);
+  const int d = nth_bit4(dm, reverse ? (uint32_t)popc(dm) - 1u - rem : rem);
+  const int tj = sq + jump_off(d), ts = sq + step_off(sq, d);
+  const int to = capture ? tj : ts;
+  const uint32_t removed = capture ? (1u << mid_square(sq, tj)) : 0u;
+  apply_move(b, sq, to, removed);
+  return n;
+}
+
+// Random draws of one stream buffered eight at a time, so that a warp can
+// generate Philox blocks for all its lanes at the same loop iteration.
+// refill() keeps at least four draws buffered; next() consumes one.
+struct DrawRing {
+  uint32_t a0, a1, a2, a3, b0, b1, b2, b3;  // slots 0-3 and 4-7
+  uint32_t k, avail;
+  uint32_t k0, k1, id0, id1, tag;
+
+  GA_HD void start(uint64_t seed, uint64_t id, uint32_t tag_) {
+    k0 = (uint32_t)seed; k1 = (uint32_t)(seed >> 32);
+    id0 = (uint32_t)id; id1 = (uint32_t)(id >> 32);
+    tag = tag_; k = 0; avail = 0;
+  }
+  GA_HD void refill() {
+    if (avail >= 4) return;
+    const uint32_t pos = k + avail;  // multiple of 4
+    uint32_t c[4] = {pos >> 2, id0, id1, tag};
+    philox4x32_10(c, k0, k1);
+    const bool hi = (pos & 4u) != 0;
+    a0 = hi ? a0 : c[0]; a1 = hi ? a1 : c[1]; a2 = hi ? a2 : c[2]; a3 = hi ? a3 : c[3];
+    b0 = hi ? c[0] : b0; b1 = hi ? c[1] : b1; b2 = hi ? c[2] : b2; b3 = hi ? c[3] : b3;
+    avail += 4;
+  }
+  // Move index in [0, n) for n >= 1; a draw is consumed only when n >= 2.
+  GA_HD uint32_t pick(uint32_t n) {
+    const bool hi = (k & 4u) != 0;
+    const uint32_t w = k & 3u;
+    const uint32_t x0 = hi ? b0 : a0, x1 = hi ? b1 : a1, x2 = hi ? b2 : a2, x3 = hi ? b3 : a3;
+    const uint32_t r = w == 0 ? x0 : (w == 1 ? x1 : (w == 2 ? x2 : x3));
+    const uint32_t use = n >= 2 ? 1u : 0u;
+    k += use;
+    avail -= use;
+    return use ? mulhi_index(r, n) : 0u;
+  }
+  GA_HD uint32_t next() {
+    const bool hi = (k & 4u) != 0;
+    const uint32_t w = k & 3u;
+    const uint32_t x0 = hi ? b0 : a0, x1 = hi ? b1 : a1, x2 = hi ? b2 : a2, x3 = hi ? b3 : a3;
+    const uint32_t r = w == 0 ? x0 : (w == 1 ? x1 : (w == 2 ? x2 : x3));
+    k++;
+    avail--;
+    return r;
+  }
+};
 
 // ------------------------------------------------------------ per-ply policies
 // Each returns the number of legal moves (0: the side to move has lost), -1 on a limit.
 
-GA_HD int ply_random(Board &b, Stream &rs) {
-  return play_ply(b, [&](uint32_t n) { return mulhi_index(rs.next(), n); });
+template <class Rng>
+GA_HD int ply_random(Board &b, Rng &rs) {
+  return play_ply_fast(b, [&](uint32_t n) { return n >= 2 ? mulhi_index(rs.next(), n) : 0u; });
 }
 
 // Reference heuristic: argmax over moves of weight + noise (first maximum
 // wins, as in src/heuristicPlayout.cpp:31-35).
-GA_HD int ply_ref_heuristic(Board &b, Stream &rs) {
+template <class Rng>
+GA_HD int ply_ref_heuristic(Board &b, Rng &rs) {
   Side s;
   make_side(b, s);
   const uint32_t J = jumpers(s);
@@ -487,7 +763,8 @@ GA_HD int ply_ref_heuristic(Board &b, Stream &rs) {
 
 constexpr uint32_t kEpsThreshold = 429496730u;  // ceil(0.1 * 2^32)
 
-GA_HD int ply_eps_greedy(Board &b, Stream &rs) {
+template <class Rng>
+GA_HD int ply_eps_greedy(Board &b, Rng &rs) {
   Side s;
   make_side(b, s);
   const uint32_t J = jumpers(s);
@@ -524,8 +801,8 @@ GA_HD int ply_eps_greedy(Board &b, Stream &rs) {
   return n;
 }
 
-template <int POLICY>
-GA_HD int ply(Board &b, Stream &rs) {
+template <int POLICY, class Rng>
+GA_HD int ply(Board &b, Rng &rs) {
   if (POLICY == 1) return ply_ref_heuristic(b, rs);
   if (POLICY == 2) return ply_eps_greedy(b, rs);
   return ply_random(b, rs);

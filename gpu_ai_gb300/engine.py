@@ -78,6 +78,8 @@ def load_library(path: str = LIB_PATH):
     lib.gpuai_random_positions.argtypes = [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint32,
                                            ctypes.c_uint32, _u32p]
     lib.gpuai_device_info.argtypes = [ctypes.c_void_p, _i32p, _i32p, _i32p]
+    lib.gpuai_set_launch.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32]
+    lib.gpuai_get_launch.argtypes = [ctypes.c_void_p, ctypes.c_int32, _i32p, _i32p, _i32p]
     for name in header_symbols():
         if name not in ("gpuai_last_error", "gpuai_destroy"):
             getattr(lib, name).restype = ctypes.c_int
@@ -169,6 +171,14 @@ class Engine:
         out = np.zeros((n, 4), dtype=np.uint32)
         _check(self.lib.gpuai_random_positions(self.ctx, seed, n, min_plies, max_plies, out.ctypes.data_as(_u32p)))
         return out
+
+    def set_launch(self, policy: int, block_threads: int, blocks_per_sm: int = 0):
+        _check(self.lib.gpuai_set_launch(self.ctx, policy, block_threads, blocks_per_sm))
+
+    def get_launch(self, policy: int = POLICY_RANDOM):
+        a, b, c = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+        _check(self.lib.gpuai_get_launch(self.ctx, policy, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
+        return {"block_threads": a.value, "blocks_per_sm": b.value, "max_blocks_per_sm": c.value}
 
     def device_info(self):
         a, b, c = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()

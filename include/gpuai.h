@@ -74,8 +74,8 @@ const char *gpuai_last_error(void);
 int gpuai_playouts(gpuai_ctx *ctx, const gpuai_board *pos, const uint32_t *reps, uint32_t npos,
                    uint64_t seed, uint64_t stream_base, int32_t policy, int8_t *out);
 
-/* Same work on device-resident buffers, enqueued on `stream` (a cudaStream_t,
- * or NULL for the context's stream) without synchronising.  d_offsets holds
+/* Same work on device-resident buffers, enqueued on `stream` (a cudaStream_t;
+ * NULL is the legacy default stream) without synchronising.  d_offsets holds
  * npos+1 exclusive prefix sums of the repetitions, or is NULL when every
  * position has `uniform_reps` playouts.  total = number of playouts.  Calls on
  * one context must be ordered on one stream: they share the context's work
@@ -100,8 +100,19 @@ int gpuai_genmoves(gpuai_ctx *ctx, const gpuai_board *pos, uint32_t n, gpuai_mov
 int gpuai_random_positions(gpuai_ctx *ctx, uint64_t seed, uint32_t n, uint32_t min_plies,
                            uint32_t max_plies, gpuai_board *out);
 
-/* Number of SMs and resident playout blocks per SM chosen for this device. */
+/* Number of SMs, and the launch shape of the uniform-random playout kernel. */
 int gpuai_device_info(gpuai_ctx *ctx, int32_t *sms, int32_t *blocks_per_sm, int32_t *block_threads);
+
+/* Launch shape of the playout kernel for `policy`: threads per block (64,
+ * 128, 256 or 512) and resident blocks per SM the persistent grid uses
+ * (0 = as many as fit).  The grid is SMs x blocks_per_sm, or fewer blocks for
+ * small batches.  Results do not depend on the launch shape.  This is the
+ * knob the autotuner sweeps; it has no counterpart in the reference, whose
+ * drivers hard-code <<<N,32>>>, <<<N/128,128>>> and the coarse grid
+ * (src/multiplePlayout.cu:77, src/singlePlayout.cu:86-99, src/coarsePlayout.cu:113-115). */
+int gpuai_set_launch(gpuai_ctx *ctx, int32_t policy, int32_t block_threads, int32_t blocks_per_sm);
+int gpuai_get_launch(gpuai_ctx *ctx, int32_t policy, int32_t *block_threads, int32_t *blocks_per_sm,
+                     int32_t *max_blocks_per_sm);
 
 #ifdef __cplusplus
 }

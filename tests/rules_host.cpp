@@ -64,6 +64,38 @@ int rh_playout(const uint32_t *pos, uint64_t seed, uint64_t id, int policy, uint
   return outcome;
 }
 
+// The same playout with the uniform-random kernel's schedule: Philox blocks
+// generated every fourth iteration (DrawRing), plies whose capture can be
+// extended deferred to every eighth iteration, as the warp loop does.
+int rh_playout_ring(const uint32_t *pos, uint64_t seed, uint64_t id, uint32_t *plies, uint32_t *draws) {
+  Board b = load(pos);
+  DrawRing rs;
+  rs.start(seed, id, 0);
+  auto pick = [&](uint32_t n) { return rs.pick(n); };
+  uint32_t p = 0;
+  int outcome = 0;
+  bool pending = false;
+  for (uint32_t it = 0;; ++it) {
+    if ((it & 3u) == 0) rs.refill();
+    int n;
+    if (pending) {
+      if ((it & 7u) != 0) continue;
+      pending = false;
+      n = play_ply_fast<false>(b, pick);
+    } else {
+      if (((b.meta >> 8) & 0xffu) >= (uint32_t)kDrawPlies) { outcome = 0; break; }
+      n = play_ply_fast<true>(b, pick);
+      if (n == kNeedSearch) { pending = true; continue; }
+    }
+    if (n == 0) { outcome = (b.meta & 1u) ? 1 : -1; break; }
+    if (n < 0) { outcome = -100; break; }
+    p++;
+  }
+  if (plies) *plies = p;
+  if (draws) *draws = rs.k;
+  return outcome;
+}
+
 void rh_random_positions(uint64_t seed, uint32_t n, uint32_t min_plies, uint32_t max_plies,
                          uint32_t *out) {
   for (uint32_t p = 0; p < n; p++) {

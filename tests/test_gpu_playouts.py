@@ -118,3 +118,24 @@ def test_device_resident_path(engine, golden_playout):
     torch.cuda.synchronize()
     np.testing.assert_array_equal(d_out.cpu().numpy(), exp)
     assert engine.status()[0] == 0
+
+
+@pytest.mark.parametrize("block,per_sm", [(64, 0), (128, 3), (256, 1), (512, 0)])
+def test_launch_shape_does_not_change_results(engine, block, per_sm):
+    pos = L.random_positions(21, 64, 0, 30)
+    reps = np.full(64, 300, dtype=np.uint32)
+    exp, _ = L.replay_batch(pos, reps, seed=21, stream_base=5)
+    old = engine.get_launch(0)
+    try:
+        engine.set_launch(0, block, per_sm)
+        got = engine.playouts(pos, reps, seed=21, stream_base=5)
+    finally:
+        engine.set_launch(0, old["block_threads"], old["blocks_per_sm"])
+    np.testing.assert_array_equal(got, exp)
+
+
+def test_set_launch_rejects_bad_shapes(engine):
+    with pytest.raises(GpuAIError):
+        engine.set_launch(0, 96, 0)
+    with pytest.raises(GpuAIError):
+        engine.set_launch(5, 256, 0)
