@@ -89,6 +89,21 @@ __global__ void __launch_bounds__(BLOCK) playout_kernel(PlayoutArgs a) {
     // every kSearchPeriod-th iteration, so that the lanes needing the longer
     // capture code run it together and the per-iteration code stays
     // branch-free for the others.
+    //
+    // Once the work counter is exhausted, every kCompactPeriod-th iteration the
+    // block packs its unfinished games (board, random-stream state, counters)
+    // into its lowest threads through shared memory; warps left without games
+    // wait at the next barrier instead of issuing empty iterations.  The loop
+    // ends for the whole block when it has no game left.
+    constexpr int kWords = 17;
+    __shared__ uint32_t s_slot[kWords][BLOCK];
+    __shared__ uint32_t s_cnt[BLOCK / 32];
+    // exhaustion flag per parity of the compaction point, so that a warp
+    // setting it for the next point cannot race a slower warp's read
+    __shared__ uint32_t s_ex[2];
+    const uint32_t warp = threadIdx.x >> 5;
+    if (threadIdx.x < 2) s_ex[threadIdx.x] = 0;
+    __syncthreads();
     DrawRing rs;
     rs.start(0, 0, 0);
     bool pending = false;
@@ -101,35 +116,81 @@ __global__ void __launch_bounds__(BLOCK) playout_kernel(PlayoutArgs a) {
           rs.start(a.seed, a.stream_base + j, 0);
           game_plies = 0;
         }
-        if (!__any_sync(kFull, have)) break;
         if (have) rs.refill();
       }
-      if (!have) continue;
-      int n;
-      if (pending) {
-        if ((it & (kSearchPeriod - 1u)) != 0) continue;
-        pending = false;
-        n = play_ply_fast<false>(b, pick);
-      } else {
-        if (((b.meta >> 8) & 0xffu) >= (uint32_t)kDrawPlies) {
-          a.out[j] = 0;
-          have = false;
-          continue;
+      do {
+        if (!have) break;
+        int n;
+        if (pending) {
+          if ((it & (kSearchPeriod - 1u)) != 0) break;
+          pending = false;
+          n = play_ply_fast<false>(b, pick);
+        } else {
+          if (((b.meta >> 8) & 0xffu) >= (uint32_t)kDrawPlies) {
+            a.out[j] = 0;
+            have = false;
+            break;
+          }
+          n = play_ply_fast<true>(b, pick);
+          if (n == kNeedSearch) {
+            pending = true;
+            break;
+          }
         }
-        n = play_ply_fast<true>(b, pick);
-        if (n == kNeedSearch) {
-          pending = true;
-          continue;
+        if (n > 0 && ++game_plies <= kMaxPlies) {
+          plies_here++;
+          break;
         }
-      }
-      if (n > 0 && ++game_plies <= kMaxPlies) {
-        plies_here++;
+        if (n < 0) atomicOr(a.status, kStatusDepth);
+        else if (n > 0) atomicOr(a.status, kStatusPlyCap);
+        a.out[j] = (int8_t)(n == 0 ? ((b.meta & 1u) ? 1 : -1) : 0);  // side to move cannot move: loses
+        have = false;
+      } while (false);
+
+      if ((it & (kCompactPeriod - 1u)) != kCompactPeriod - 1u) {
+        // a warp with no game left skips ahead to the block's next compaction point
+        if (exhausted && !__any_sync(kFull, have)) it = (it | (kCompactPeriod - 1u)) - 1u;
         continue;
       }
-      if (n < 0) atomicOr(a.status, kStatusDepth);
-      else if (n > 0) atomicOr(a.status, kStatusPlyCap);
-      a.out[j] = (int8_t)(n == 0 ? ((b.meta & 1u) ? 1 : -1) : 0);  // side to move cannot move: loses
-      have = false;
+      const uint32_t parity = (it / kCompactPeriod) & 1u;
+      if (exhausted && lane == 0) s_ex[parity] = 1;
+      __syncthreads();
+      if (!s_ex[parity]) continue;  // block-uniform: the work counter is not exhausted yet
+      const uint32_t m = __ballot_sync(kFull, have);
+      if (lane == 0) s_cnt[warp] = __popc(m);
+      __syncthreads();
+      uint32_t total = 0, before = 0, busy_warps = 0;
+#pragma unroll
+      for (uint32_t w = 0; w < BLOCK / 32; w++) {
+        const uint32_t c = s_cnt[w];
+        before += w < warp ? c : 0u;
+        total += c;
+        busy_warps += c ? 1u : 0u;
+      }
+      if (total == 0) break;
+      exhausted = true;
+      if ((total + 31u) / 32u >= busy_warps) continue;  // packing would free no warp
+      if (have) {
+        const uint32_t slot = before + __popc(m & ((1u << lane) - 1u));
+        const uint32_t v[kWords] = {b.p1, b.p2, b.kings, b.meta, j, game_plies, pending ? 1u : 0u,
+                                    rs.a0, rs.a1, rs.a2, rs.a3, rs.b0, rs.b1, rs.b2, rs.b3, rs.k, rs.avail};
+#pragma unroll
+        for (int q = 0; q < kWords; q++) s_slot[q][slot] = v[q];
+      }
+      __syncthreads();
+      have = threadIdx.x < total;
+      if (have) {
+        const uint32_t t = threadIdx.x;
+        b.p1 = s_slot[0][t]; b.p2 = s_slot[1][t]; b.kings = s_slot[2][t]; b.meta = s_slot[3][t];
+        j = s_slot[4][t];
+        game_plies = s_slot[5][t];
+        pending = s_slot[6][t] != 0;
+        rs.start(a.seed, a.stream_base + j, 0);
+        rs.a0 = s_slot[7][t]; rs.a1 = s_slot[8][t]; rs.a2 = s_slot[9][t]; rs.a3 = s_slot[10][t];
+        rs.b0 = s_slot[11][t]; rs.b1 = s_slot[12][t]; rs.b2 = s_slot[13][t]; rs.b3 = s_slot[14][t];
+        rs.k = s_slot[15][t];
+        rs.avail = s_slot[16][t];
+      }
     }
   } else {
     Stream rs;
