@@ -92,6 +92,12 @@ struct Control {
 
 }  // namespace
 
+namespace ga {
+// Records `msg` as the calling thread's gpuai_last_error() and returns code
+// (for entry points defined in other translation units).
+int record_error(int code, const char *msg) { return fail(code, "%s", msg); }
+}  // namespace ga
+
 struct gpuai_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;

@@ -42,4 +42,7 @@ cudaError_t launch_genmoves(const Board *pos, uint32_t n, void *out, uint32_t ma
 cudaError_t launch_random_positions(uint64_t seed, uint32_t n, uint32_t min_plies,
                                     uint32_t max_plies, Board *out, cudaStream_t s);
 
+// Sets the calling thread's gpuai_last_error() message; returns code.
+int record_error(int code, const char *msg);
+
 }  // namespace ga

@@ -114,6 +114,29 @@ int gpuai_set_launch(gpuai_ctx *ctx, int32_t policy, int32_t block_threads, int3
 int gpuai_get_launch(gpuai_ctx *ctx, int32_t policy, int32_t *block_threads, int32_t *blocks_per_sm,
                      int32_t *max_blocks_per_sm);
 
+/* Playouts that allocate no device memory, for callers that may not call
+ * cudaMalloc: for example a search server that reserves the whole device
+ * memory budget for its trees up front, or a move loop with a hard per-move
+ * deadline that must never wait on the allocator.  It has no counterpart in
+ * the reference.  d_pos (npos boards) and d_out (one int8 outcome per playout)
+ * are device buffers the caller already owns; reps is a HOST array of
+ * repetitions (NULL: one playout per board); results equal gpuai_playouts with
+ * the same seed and stream_base.  The work counter, status word and the
+ * repetition prefix sums live in one statically allocated device array per
+ * GPU, sized for at most GPUAI_NOALLOC_MAX_POSITIONS positions (about 64 KiB,
+ * held until the process exits); larger npos is rejected with
+ * GPUAI_ERR_INVALID.  No context is needed: the call runs on the current
+ * device and `stream` (NULL: the legacy default stream) and returns after the
+ * playouts finished.  The first call on a device looks up that array's device
+ * address; make that first call before any stream capture.  All calls share
+ * the array, which keeps the previous call's contents (the call clears what
+ * must start at zero); calls on one device are serialised by the library,
+ * and launches that overlapped on the GPU would race on it. */
+#define GPUAI_NOALLOC_MAX_POSITIONS 16384
+int gpuai_playouts_noalloc(const gpuai_board *d_pos, const uint32_t *reps, uint32_t npos,
+                           uint64_t seed, uint64_t stream_base, int32_t policy, int8_t *d_out,
+                           void *stream);
+
 #ifdef __cplusplus
 }
 #endif
