@@ -10,7 +10,8 @@ streams (stream_base advances), so no step repeats work.
          CUDA-event time of the K timed launches (L2 flushed between steps)
   e2e    the same metric through the public C ABI call gpuai_playouts() on
          host buffers: H2D of boards + offsets and D2H of outcomes every step
-  roofline  integer-issue roofline of the playout kernel
+  roofline  integer-issue roofline of the playout kernel: plies/s x OPS_PER_PLY
+         lane operations against SMs x 128 lanes x the maximum SM clock
   cpu_baseline  the reference's HostPlayoutDriver (built from its sources
          where present, else the oracle's restatement of it) on the host's
          cores, on a bounded sample of the same positions
@@ -50,8 +51,8 @@ WORKLOAD = {
 # the algorithmic work unit of the integer-issue roofline.
 OPS_PER_PLY = 260.0
 # DRAM bytes per launch of the playout kernel from one ncu capture
-# (dram__bytes_read.sum + dram__bytes_write.sum); None until captured.
-TRAFFIC_BYTES = None
+# (dram__bytes_read.sum + dram__bytes_write.sum).
+TRAFFIC_BYTES = 39424  # one ncu capture of the benchmark launch: 39.4 KB read, 0 B written
 
 
 def measured_peaks():
