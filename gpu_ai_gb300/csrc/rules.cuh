@@ -25,8 +25,10 @@
 
 #if defined(__CUDACC__)
 #define GA_HD __host__ __device__ __forceinline__
+#define GA_UNROLL _Pragma("unroll")
 #else
 #define GA_HD inline
+#define GA_UNROLL
 #endif
 
 namespace ga {
@@ -149,7 +151,7 @@ GA_HD void direct_masks(const Side &s, uint32_t md[4]) {
 // the sequence (the cycle check of src/state.cu:134-139).
 GA_HD uint32_t capture_dirs(const Side &s, int t, bool king, uint32_t visited) {
   uint32_t v[4];
-#pragma unroll
+GA_UNROLL
   for (int d = 0; d < 4; d++) {
     uint32_t can = (s.jd[d] >> t) & 1u;
     uint32_t land = (uint32_t)(t + jump_off(d)) & 31u;
@@ -242,7 +244,7 @@ GA_HD bool promotes(const Board &b, int from, int to) {
 GA_HD void pack_move(const Board &b, int from, int to, int jumps, uint32_t dirs, uint32_t w[8]) {
   w[0] = (uint32_t)from | ((uint32_t)to << 8) | ((uint32_t)jumps << 16) |
          ((promotes(b, from, to) ? 1u : 0u) << 24);
-#pragma unroll
+GA_UNROLL
   for (int q = 1; q < 7; q++) w[q] = 0xffffffffu;
   w[7] = 0;
   int t = from;
@@ -261,7 +263,7 @@ GA_HD void pack_move(const Board &b, int from, int to, int jumps, uint32_t dirs,
 
 // Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11).
 GA_HD void philox4x32_10(uint32_t c[4], uint32_t k0, uint32_t k1) {
-#pragma unroll
+GA_UNROLL
   for (int r = 0; r < 10; r++) {
 #if defined(__CUDA_ARCH__)
     uint32_t hi0 = __umulhi(0xD2511F53u, c[0]), lo0 = 0xD2511F53u * c[0];
@@ -356,7 +358,7 @@ GA_HD int for_each_move(const Side &s, uint32_t J, Fn &&fn) {
   direct_masks(s, md);
   for (uint32_t any = md[0] | md[1] | md[2] | md[3]; any; any &= any - 1) {
     const int sq = ctz(any);
-#pragma unroll
+GA_UNROLL
     for (int d = 0; d < 4; d++)
       if ((md[d] >> sq) & 1u) {
         n++;
@@ -538,7 +540,7 @@ template <int FA, int FB>
 GA_HD ManTree man_tree(const Side &s) {
   const uint32_t A = s.jd[FA], B = s.jd[FB], any = A | B;
   uint32_t c0 = ~0u, c1 = 0u, c2 = 0u;
-#pragma unroll
+GA_UNROLL
   for (int r = 0; r < 2; r++) {
     const uint32_t a0 = jump2_back<FA>(c0) & A, a1 = jump2_back<FA>(c1) & A, a2 = jump2_back<FA>(c2) & A;
     const uint32_t b0 = jump2_back<FB>(c0) & B, b1 = jump2_back<FB>(c1) & B, b2 = jump2_back<FB>(c2) & B;
@@ -652,7 +654,7 @@ GA_HD int play_ply_fast(Board &b, Pick &&pick) {
   const uint32_t i = pick((uint32_t)n);
   // square of move i: the largest x with (moves from squares < x) <= i
   uint32_t lo = 0, clo = 0;
-#pragma unroll
+GA_UNROLL
   for (uint32_t st = 16; st >= 1; st >>= 1) {
     const uint32_t mid = lo + st;
     const uint32_t L = (1u << mid) - 1u;

@@ -8,9 +8,11 @@
 //   State::move                           src/state.cu:57-92
 //   HostPlayoutDriver::runPlayouts        src/playout.cpp:17-32
 //   HostHeuristicPlayoutDriver::runPlayouts src/heuristicPlayout.cpp:12-48
+//   GameTree::select / update               src/mcts.cpp:63-191
 // The tests use it to pin the plain-C restatement in oracle.c.
 #include "state.hpp"
 #include "playout.hpp"
+#include "mcts.hpp"
 
 #include <cstdint>
 #include <cstdlib>
@@ -122,6 +124,49 @@ void ref_host_heuristic_playouts(const uint32_t *b16, uint32_t n, int8_t *out) {
   HostHeuristicPlayoutDriver d;
   std::vector<PlayerId> r = d.runPlayouts(states);
   for (uint32_t i = 0; i < n; i++) out[i] = outcome(r[i]);
+}
+
+// Deterministic stand-in outcome of a playout from a board record, shared
+// with the project's tree test so both trees see the same results.
+static PlayerId fake_outcome(const uint32_t *b, uint64_t salt) {
+  uint64_t x = ((uint64_t)b[0] | ((uint64_t)b[1] << 32)) ^ ((uint64_t)b[2] * 0x9E3779B97F4A7C15ull) ^
+               ((uint64_t)b[3] * 0xC2B2AE3D27D4EB4Full) ^ salt;
+  x ^= x >> 31; x *= 0x7FB5D329728EA185ull; x ^= x >> 27; x *= 0x81DADEF4BC2DD44Dull; x ^= x >> 33;
+  const unsigned r = (unsigned)(x % 7);
+  return r < 3 ? PLAYER_1 : (r < 6 ? PLAYER_2 : PLAYER_NONE);
+}
+
+// Runs `iters` rounds of select(trials[i]) / update on the reference's
+// GameTree from `root`, outcomes from fake_outcome; writes per root child
+// {total, wins P1, wins P2} and returns the number of children.
+int ref_tree_run(const uint32_t *root, const uint32_t *trials, int iters, uint64_t salt, uint32_t *out,
+                 int max_children) {
+  GameTree tree(from_b16(root));
+  for (int i = 0; i < iters; i++) {
+    std::vector<State> leaves = tree.select(trials[i]);
+    std::vector<PlayerId> res(leaves.size());
+    for (size_t k = 0; k < leaves.size(); k++) {
+      uint32_t b[4];
+      to_b16(leaves[k], b);
+      res[k] = fake_outcome(b, salt);
+    }
+    tree.update(res);
+  }
+  // child statistics through the public interface: score() = wins / total
+  State s = from_b16(root);
+  std::vector<Move> moves = s.getMoves();
+  int n = 0;
+  for (const Move &m : moves) {
+    if (n >= max_children) break;
+    std::shared_ptr<GameTree> child = tree.move(m);
+    const unsigned total = child->getTotalTrials();
+    const bool stats = total > 0 && !child->state.isGameOver();  // getScore is wins/total there
+    out[3 * n] = total;
+    out[3 * n + 1] = stats ? (uint32_t)(child->getScore(PLAYER_1) * total + 0.5) : 0u;
+    out[3 * n + 2] = stats ? (uint32_t)(child->getScore(PLAYER_2) * total + 0.5) : 0u;
+    n++;
+  }
+  return n;
 }
 
 }  // extern "C"
