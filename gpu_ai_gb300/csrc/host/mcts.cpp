@@ -148,6 +148,13 @@ void GameTree::select_rec(int32_t n, unsigned trials, std::vector<State> &out) {
     wsum += w[i];
     if (nodes_[first + (int32_t)i].total == 0) untried++;
   }
+  // All weights zero (a parent with one finished playout whose children have
+  // not won yet, e.g. a forced move): the proportional split below would be
+  // 0/0, so the weights count as equal.
+  if (untried == 0 && !(wsum > 0 && std::isfinite(wsum))) {
+    for (uint32_t i = 0; i < nc; i++) w[i] = 1.0;
+    wsum = (double)nc;
+  }
   unsigned assigned = 0;
   for (uint32_t i = 0; i < nc; i++) {
     if (untried > 0) give[i] = nodes_[first + (int32_t)i].total == 0 ? trials / untried : 0;

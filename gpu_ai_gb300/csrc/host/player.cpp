@@ -36,7 +36,9 @@ Move MCTSPlayer::getMove(const State &state, bool verbose) {
   std::lock_guard<std::mutex> lock(mu_);
   if (!error_.empty()) throw std::runtime_error(error_);
   if (!tree_->expanded()) {
-    // the worker has not finished a batch yet: expand with one small batch here
+    // the worker has not finished a batch on this tree yet: run one small
+    // batch here and drop the worker's batch in flight (its select is stale)
+    updateCancelled_ = true;
     std::vector<State> leaves = tree_->select(64);
     tree_->update(driver_->runPlayouts(leaves));
   }

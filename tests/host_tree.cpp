@@ -73,4 +73,25 @@ int ht_tree_reroot(const uint32_t *root, unsigned trials, int iters, uint64_t sa
   return tree.state() == t ? 0 : -1;
 }
 
+// A forced move whose only child has one finished, lost playout while the
+// parent has one playout in total (reached when an expanding select's update
+// was cancelled): every UCB1 weight is zero.  Returns 0 when the next select
+// still places all its trials.
+int ht_zero_weights(const uint32_t *root) {
+  State s;
+  s.b = gpuai_board{root[0], root[1], root[2], root[3]};
+  if (s.getMoves().size() != 1) return -2;
+  GameTree tree(s);
+  tree.select(2);  // expands the root; its update is dropped
+  std::vector<State> one = tree.select(1);
+  tree.update(std::vector<PlayerId>(one.size(), s.getNextTurn()));
+  try {
+    std::vector<State> l = tree.select(5);
+    tree.update(std::vector<PlayerId>(l.size(), PLAYER_NONE));
+    return l.size() == 5 ? 0 : -1;
+  } catch (const std::exception &) {
+    return -1;
+  }
+}
+
 }  // extern "C"

@@ -30,6 +30,7 @@ def ht():
     lib = ctypes.CDLL(SO)
     lib.ht_tree_run.argtypes = [u32p, u32p, ctypes.c_int, ctypes.c_uint64, u32p, ctypes.c_int, ctypes.c_int, u32p]
     lib.ht_tree_reroot.argtypes = [u32p, ctypes.c_uint, ctypes.c_int, ctypes.c_uint64, u32p, u32p]
+    lib.ht_zero_weights.argtypes = [u32p]
     return lib
 
 
@@ -70,3 +71,12 @@ def test_reroot_keeps_subtree(ht):
     before, after = ctypes.c_uint32(), ctypes.c_uint32()
     assert ht.ht_tree_reroot(root.ctypes.data_as(u32p), 500, 10, 9, ctypes.byref(before), ctypes.byref(after)) == 0
     assert before.value == after.value > 0
+
+
+def test_all_zero_ucb_weights(ht):
+    from golden_boards import crafted_boards
+    b = crafted_boards()
+    forced = [r for r in b if L.genmoves(r)[1][0] == 1]
+    assert forced
+    root = np.ascontiguousarray(forced[0], dtype=np.uint32)
+    assert ht.ht_zero_weights(root.ctypes.data_as(u32p)) == 0
