@@ -170,9 +170,16 @@ def max_over_ranks(x, world):
         return x
     import torch
     import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def rank_stream_base(rank):
+    """First random-stream id of a rank: replicas use disjoint id ranges
+    (2^40 playouts per rank) so no two ranks replay the same playouts."""
+    return rank << 40
 
 
 def run_reference(args):
@@ -224,7 +231,7 @@ def run_ours(args):
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
     sid = stream.cuda_stream
-    base = (rank << 40)
+    base = rank_stream_base(rank)
 
     def step(k):
         eng.playouts_device(d_pos.data_ptr(), None, N_POS, REPS, TOTAL, 0x5EED, base + k * TOTAL, 0,
