@@ -15,6 +15,7 @@ from .engine import (  # noqa: F401
     POLICY_REF_HEURISTIC,
     START_BOARD,
     Engine,
+    Searches,
     GpuAIError,
     header_symbols,
     load_library,
@@ -22,6 +23,7 @@ from .engine import (  # noqa: F401
 
 __all__ = [
     "Engine",
+    "Searches",
     "GpuAIError",
     "load_library",
     "header_symbols",

@@ -24,6 +24,13 @@ __device__ __forceinline__ uint32_t position_of(const PlayoutArgs &a, uint32_t j
   return lo;
 }
 
+// Random-stream id of playout j, which plays position p.
+__device__ __forceinline__ uint64_t stream_of(const PlayoutArgs &a, uint32_t p, uint32_t j) {
+  if (a.pos_stream == nullptr) return a.stream_base + j;
+  const uint32_t first = a.offsets ? __ldg(&a.offsets[p]) : p * a.uniform_reps;
+  return __ldg(&a.pos_stream[p]) + (j - first);
+}
+
 __device__ __forceinline__ Board load_board(const Board *p) {
   uint4 v = __ldg(reinterpret_cast<const uint4 *>(p));
   Board b;
@@ -76,6 +83,10 @@ __device__ __forceinline__ bool step_game(const PlayoutArgs &a, Board &b, Rng &r
 
 template <int POLICY, int BLOCK>
 __global__ void __launch_bounds__(BLOCK) playout_kernel(PlayoutArgs a) {
+  if (a.dev_sizes != nullptr) {
+    a.npos = __ldg(&a.dev_sizes[0]);
+    a.total = __ldg(&a.dev_sizes[1]);
+  }
   const uint32_t lane = threadIdx.x & 31u;
   Board b = {0, 0, 0, 0};
   uint32_t j = 0, plies_here = 0, game_plies = 0;
@@ -112,8 +123,9 @@ __global__ void __launch_bounds__(BLOCK) playout_kernel(PlayoutArgs a) {
       if ((it & 3u) == 0) {
         if (claim(a, have, j, exhausted, lane)) {
           have = true;
-          b = load_board(a.pos + position_of(a, j));
-          rs.start(a.seed, a.stream_base + j, 0);
+          const uint32_t p = position_of(a, j);
+          b = load_board(a.pos + p);
+          rs.start(a.seed, stream_of(a, p, j), 0);
           game_plies = 0;
         }
         if (have) rs.refill();
@@ -185,7 +197,7 @@ __global__ void __launch_bounds__(BLOCK) playout_kernel(PlayoutArgs a) {
         j = s_slot[4][t];
         game_plies = s_slot[5][t];
         pending = s_slot[6][t] != 0;
-        rs.start(a.seed, a.stream_base + j, 0);
+        rs.start(a.seed, stream_of(a, position_of(a, j), j), 0);  // then the buffered draws and counter
         rs.a0 = s_slot[7][t]; rs.a1 = s_slot[8][t]; rs.a2 = s_slot[9][t]; rs.a3 = s_slot[10][t];
         rs.b0 = s_slot[11][t]; rs.b1 = s_slot[12][t]; rs.b2 = s_slot[13][t]; rs.b3 = s_slot[14][t];
         rs.k = s_slot[15][t];
@@ -198,8 +210,9 @@ __global__ void __launch_bounds__(BLOCK) playout_kernel(PlayoutArgs a) {
     for (;;) {
       if (claim(a, have, j, exhausted, lane)) {
         have = true;
-        b = load_board(a.pos + position_of(a, j));
-        rs.init(a.seed, a.stream_base + j, 0);
+        const uint32_t p = position_of(a, j);
+        b = load_board(a.pos + p);
+        rs.init(a.seed, stream_of(a, p, j), 0);
         game_plies = 0;
       }
       if (!__any_sync(kFull, have)) break;

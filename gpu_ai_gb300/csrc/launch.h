@@ -30,6 +30,13 @@ struct PlayoutArgs {
   uint32_t *counter;              // work counter, zero before launch
   uint32_t *status;               // status bits, zero before launch
   unsigned long long *plies;      // plies played (optional)
+  // Optional: first random-stream id of each position (playout j of position
+  // p then uses pos_stream[p] + j - first playout of p); nullptr means
+  // stream_base + j.
+  const uint64_t *pos_stream = nullptr;
+  // Optional: {npos, total} read from device memory at kernel start, for
+  // launches inside a CUDA graph whose sizes are computed on the device.
+  const uint32_t *dev_sizes = nullptr;
 };
 
 // Playout kernels are instantiated for blocks of 64, 128, 256 and 512 threads.

@@ -1,0 +1,584 @@
+// search.cu -- many MCTS searches at once, with their trees in device memory.
+//
+// The reference runs one search per MCTSPlayer on the host and sends each leaf
+// batch to the GPU (src/player.cpp:134-150, src/mcts.cpp:63-191).  Here all
+// searches' trees live in one node pool in HBM (structure of arrays, one
+// contiguous node range per search) and one step advances every active
+// search:
+//
+//   quota_kernel     leaf slots per search this step (min(Q, remaining
+//                    budget)), prefix sums, total leaves / playouts
+//   select_kernel    one warp per search: Q sequential UCT descents with
+//                    virtual loss, expanding a leaf (all children at once)
+//                    the second time it is reached; writes leaf boards and
+//                    per-leaf random-stream ids
+//   playout_kernel   the playout kernel on the leaf boards (sizes and stream
+//                    ids read from device memory)
+//   backprop_kernel  one thread per leaf: visits and score up the path,
+//                    virtual loss removed
+//
+// The four launches are replayed as one CUDA graph per step.  Because each
+// search is selected by a single warp in a fixed order and its playouts use
+// its own stream ids, a search's tree and result do not depend on which other
+// searches share the steps.
+#include "../../include/gpuai.h"
+#include "launch.h"
+#include "rules.cuh"
+
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <iterator>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+namespace ga {
+namespace {
+
+constexpr uint32_t kExpanded = 1u, kTerminal = 2u;
+constexpr int kMaxSelectDepth = 512;
+constexpr uint32_t kStatusSelectDepth = 8u;
+constexpr float kUcbC = 1.41421356f;
+
+struct Pool {  // one entry per node
+  uint4 *board;
+  int32_t *parent, *first_child, *nchild;
+  uint32_t *visits, *score2, *vloss, *state, *move, *removed;
+};
+
+struct Table {  // one entry per search slot
+  int32_t *root, *node_next, *node_end;
+  unsigned long long *stream_next, *budget, *done;
+  uint32_t *quota_off;  // slots + 1
+};
+
+struct Leaves {
+  uint4 *board;
+  int32_t *node, *search;
+  unsigned long long *stream;
+  int8_t *out;
+  uint32_t *sizes;  // {leaves, playouts}
+};
+
+__device__ __forceinline__ bool board_terminal(const Board &b) {
+  if (((b.meta >> 8) & 0xffu) >= (uint32_t)kDrawPlies) return true;
+  Side s;
+  make_side(b, s);
+  return count_moves(s, jumpers(s)) == 0;
+}
+
+// Leaf slots per search and their prefix sums (one block).
+__global__ void __launch_bounds__(1024) quota_kernel(Table t, uint32_t slots, uint32_t Q, uint32_t ppl, Leaves l) {
+  __shared__ uint32_t warp_sum[32];
+  __shared__ uint32_t carry;
+  const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+  if (tid == 0) carry = 0;
+  __syncthreads();
+  for (uint32_t base = 0; base < slots; base += 1024) {
+    const uint32_t s = base + tid;
+    uint32_t q = 0;
+    if (s < slots && t.root[s] >= 0) {
+      const unsigned long long b = t.budget[s], d = t.done[s];
+      if (d < b) {
+        const unsigned long long need = (b - d + ppl - 1) / ppl;
+        q = need < Q ? (uint32_t)need : Q;
+      }
+    }
+    uint32_t v = q;
+    for (uint32_t o = 1; o < 32; o <<= 1) {
+      const uint32_t n = __shfl_up_sync(0xffffffffu, v, o);
+      if (lane >= o) v += n;
+    }
+    if (lane == 31) warp_sum[warp] = v;
+    __syncthreads();
+    if (warp == 0) {
+      uint32_t w = warp_sum[lane];
+      for (uint32_t o = 1; o < 32; o <<= 1) {
+        const uint32_t n = __shfl_up_sync(0xffffffffu, w, o);
+        if (lane >= o) w += n;
+      }
+      warp_sum[lane] = w;
+    }
+    __syncthreads();
+    const uint32_t excl = v - q + (warp ? warp_sum[warp - 1] : 0u);
+    if (s < slots) t.quota_off[s] = carry + excl;
+    __syncthreads();
+    if (tid == 0) carry += warp_sum[31];
+    __syncthreads();
+  }
+  if (tid == 0) {
+    t.quota_off[slots] = carry;
+    l.sizes[0] = carry;
+    l.sizes[1] = carry * ppl;
+  }
+}
+
+// Creates all children of node n (lane 0 writes, the warp waits); false when
+// the search's node range is full.
+__device__ bool expand(const Pool &p, const Table &t, uint32_t s, int32_t n, uint32_t lane) {
+  int ok = 0;
+  if (lane == 0) {
+    const uint4 bv = p.board[n];
+    const Board b{bv.x, bv.y, bv.z, bv.w};
+    Side sd;
+    make_side(b, sd);
+    const uint32_t J = jumpers(sd);
+    const int k = count_moves(sd, J);
+    const int32_t base = t.node_next[s];
+    if (k > 0 && base + k <= t.node_end[s]) {
+      t.node_next[s] = base + k;
+      int32_t c = base;
+      for_each_move(sd, J, [&](int from, int to, uint32_t removed, int jumps, uint32_t) {
+        Board cb = b;
+        apply_move(cb, from, to, removed);
+        p.board[c] = make_uint4(cb.p1, cb.p2, cb.kings, cb.meta);
+        p.parent[c] = n;
+        p.first_child[c] = -1;
+        p.nchild[c] = 0;
+        p.visits[c] = 0;
+        p.score2[c] = 0;
+        p.vloss[c] = 0;
+        p.state[c] = board_terminal(cb) ? kTerminal : 0u;
+        p.move[c] = (uint32_t)from | ((uint32_t)to << 8) | ((uint32_t)jumps << 16) |
+                    ((promotes(b, from, to) ? 1u : 0u) << 24);
+        p.removed[c] = removed;
+        c++;
+        return false;
+      });
+      p.first_child[n] = base;
+      p.nchild[n] = k;
+      p.state[n] |= kExpanded;
+      ok = 1;
+    }
+  }
+  ok = __shfl_sync(0xffffffffu, ok, 0);
+  __syncwarp();
+  return ok != 0;
+}
+
+// One warp per search: Q sequential descents with virtual loss.
+__global__ void __launch_bounds__(256) select_kernel(Pool p, Table t, Leaves l, uint32_t slots, uint32_t ppl,
+                                                     uint32_t *status) {
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (s >= slots) return;
+  const int32_t root = t.root[s];
+  if (root < 0) return;
+  const uint32_t off = t.quota_off[s], q = t.quota_off[s + 1] - off;
+  for (uint32_t i = 0; i < q; i++) {
+    int32_t n = root;
+    for (int depth = 0;; depth++) {
+      const uint32_t st = p.state[n];
+      if (st & kTerminal) break;
+      if (!(st & kExpanded)) {
+        if (n != root && p.visits[n] == 0) break;  // a fresh leaf plays out first
+        if (!expand(p, t, s, n, lane)) break;     // node range full: play out from n
+      }
+      if (depth >= kMaxSelectDepth) {
+        if (lane == 0) atomicOr(status, kStatusSelectDepth);
+        break;
+      }
+      // UCB1 with virtual loss over the children; first best on ties
+      const int32_t first = p.first_child[n], k = p.nchild[n];
+      uint32_t tot = 0;
+      for (int32_t c = (int32_t)lane; c < k; c += 32) tot += p.visits[first + c] + p.vloss[first + c];
+      for (int o = 16; o > 0; o >>= 1) tot += __shfl_xor_sync(0xffffffffu, tot, o);
+      const float lnN = logf((float)tot + 1.0f);
+      float best = -1.0f;
+      int32_t bi = 0x7fffffff;
+      for (int32_t c = (int32_t)lane; c < k; c += 32) {
+        const uint32_t d = p.visits[first + c] + p.vloss[first + c];
+        const float v = d == 0 ? 3.0e38f
+                               : 0.5f * (float)p.score2[first + c] / (float)d + kUcbC * sqrtf(lnN / (float)d);
+        if (v > best) {
+          best = v;
+          bi = c;
+        }
+      }
+      for (int o = 16; o > 0; o >>= 1) {
+        const float ov = __shfl_xor_sync(0xffffffffu, best, o);
+        const int32_t oi = __shfl_xor_sync(0xffffffffu, bi, o);
+        if (ov > best || (ov == best && oi < bi)) {
+          best = ov;
+          bi = oi;
+        }
+      }
+      n = first + bi;
+      if (lane == 0) p.vloss[n] += 1u;
+      __syncwarp();
+    }
+    if (lane == 0) {
+      const uint32_t o = off + i;
+      l.board[o] = p.board[n];
+      l.node[o] = n;
+      l.search[o] = (int32_t)s;
+      l.stream[o] = t.stream_next[s];
+      t.stream_next[s] += ppl;
+    }
+    __syncwarp();
+  }
+}
+
+// One thread per leaf: outcomes up the path (score in half points for the
+// player who made the move into each node).
+__global__ void backprop_kernel(Pool p, Table t, Leaves l, uint32_t ppl, uint32_t max_leaves) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= max_leaves || i >= l.sizes[0]) return;
+  const int32_t s = l.search[i];
+  const int32_t root = t.root[s];
+  uint32_t w1 = 0, w2 = 0, dr = 0;
+  for (uint32_t k = 0; k < ppl; k++) {
+    const int8_t o = l.out[(size_t)i * ppl + k];
+    w1 += o > 0;
+    w2 += o < 0;
+    dr += o == 0;
+  }
+  for (int32_t n = l.node[i]; n >= 0; n = p.parent[n]) {
+    const uint32_t mover = (p.board[n].w & 1u) ^ 1u;  // 0: PLAYER_1 moved into n
+    atomicAdd(&p.visits[n], ppl);
+    atomicAdd(&p.score2[n], 2u * (mover == 0 ? w1 : w2) + dr);
+    if (n != root) atomicSub(&p.vloss[n], 1u);
+  }
+  atomicAdd(&t.done[s], (unsigned long long)ppl);
+}
+
+__global__ void init_search_kernel(Pool p, Table t, int32_t slot, int32_t start, int32_t cap, uint4 board,
+                                   unsigned long long budget, unsigned long long stream_base) {
+  p.board[start] = board;
+  p.parent[start] = -1;
+  p.first_child[start] = -1;
+  p.nchild[start] = 0;
+  p.visits[start] = 0;
+  p.score2[start] = 0;
+  p.vloss[start] = 0;
+  const Board b{board.x, board.y, board.z, board.w};
+  p.state[start] = board_terminal(b) ? kTerminal : 0u;
+  p.move[start] = 0;
+  p.removed[start] = 0;
+  t.root[slot] = start;
+  t.node_next[slot] = start + 1;
+  t.node_end[slot] = start + cap;
+  t.stream_next[slot] = stream_base;
+  t.budget[slot] = budget;
+  t.done[slot] = 0;
+}
+
+__global__ void remove_search_kernel(Table t, int32_t slot) { t.root[slot] = -1; }
+
+}  // namespace
+}  // namespace ga
+
+using namespace ga;
+
+struct gpuai_searches {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  uint32_t slots = 0, pool_nodes = 0, qmax = 0, ppl = 1;
+  int32_t policy = 0;
+  uint64_t seed = 0;
+  int sms = 0, blocks_per_sm = 1;
+  Pool pool{};
+  Table tab{};
+  Leaves leaves{};
+  uint32_t *ctl = nullptr;  // counter, status, plies (2 words)
+  std::map<uint32_t, uint32_t> free_ranges;  // start -> length
+  std::vector<int32_t> start, cap;           // per slot; start -1 = free slot
+  cudaGraphExec_t graph = nullptr;
+  uint32_t graph_q = 0;
+  std::mutex mu;
+  std::vector<void *> allocations;
+};
+
+namespace {
+
+int err(int code, const std::string &m) { return ga::record_error(code, m.c_str()); }
+int cuda_err(cudaError_t e, const char *what) {
+  return err(e == cudaErrorMemoryAllocation ? GPUAI_ERR_OOM : GPUAI_ERR_CUDA,
+             std::string("searches: ") + what + ": " + cudaGetErrorString(e));
+}
+
+#define SCK(call, what)                                   \
+  do {                                                    \
+    cudaError_t e_ = (call);                              \
+    if (e_ != cudaSuccess) return cuda_err(e_, what);     \
+  } while (0)
+
+template <class T>
+cudaError_t dalloc(gpuai_searches *s, T **p, size_t n) {
+  void *q = nullptr;
+  cudaError_t e = cudaMalloc(&q, n * sizeof(T) + 16);
+  if (e == cudaSuccess) {
+    s->allocations.push_back(q);
+    *p = static_cast<T *>(q);
+  }
+  return e;
+}
+
+int enqueue_step(gpuai_searches *s, uint32_t q) {
+  const cudaStream_t st = s->stream;
+  quota_kernel<<<1, 1024, 0, st>>>(s->tab, s->slots, q, s->ppl, s->leaves);
+  const uint32_t sel_threads = s->slots * 32u;
+  select_kernel<<<(sel_threads + 255) / 256, 256, 0, st>>>(s->pool, s->tab, s->leaves, s->slots, s->ppl, s->ctl + 1);
+  SCK(cudaMemsetAsync(s->ctl, 0, 4 * sizeof(uint32_t), st), "reset work counter");
+  PlayoutArgs a;
+  a.pos = reinterpret_cast<const Board *>(s->leaves.board);
+  a.offsets = nullptr;
+  a.npos = 0;
+  a.uniform_reps = s->ppl;
+  a.total = 0;
+  a.seed = s->seed;
+  a.stream_base = 0;
+  a.out = s->leaves.out;
+  a.counter = s->ctl;
+  a.status = s->ctl + 1;
+  a.plies = nullptr;
+  a.pos_stream = reinterpret_cast<const uint64_t *>(s->leaves.stream);
+  a.dev_sizes = s->leaves.sizes;
+  SCK(launch_playouts(a, s->policy, kPlayoutBlock, s->sms * s->blocks_per_sm, st), "playout kernel launch");
+  const uint32_t max_leaves = s->slots * s->qmax;
+  backprop_kernel<<<(max_leaves + 255) / 256, 256, 0, st>>>(s->pool, s->tab, s->leaves, s->ppl, max_leaves);
+  SCK(cudaGetLastError(), "search kernel launch");
+  return GPUAI_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int gpuai_searches_create(int device, uint32_t max_searches, uint32_t pool_nodes, uint32_t max_leaves_per_step,
+                          uint32_t playouts_per_leaf, int32_t policy, uint64_t seed, gpuai_searches **out) {
+  if (!out) return err(GPUAI_ERR_INVALID, "gpuai_searches_create: out is NULL");
+  *out = nullptr;
+  if (max_searches == 0 || pool_nodes == 0 || max_leaves_per_step == 0 || playouts_per_leaf == 0)
+    return err(GPUAI_ERR_INVALID, "gpuai_searches_create: zero size");
+  if (policy < 0 || policy > 2) return err(GPUAI_ERR_INVALID, "gpuai_searches_create: unknown policy");
+  if ((uint64_t)max_searches * max_leaves_per_step * playouts_per_leaf > 0x7fffffffull || pool_nodes > 0x7fffffffu)
+    return err(GPUAI_ERR_INVALID, "gpuai_searches_create: sizes exceed 2^31");
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || device < 0 || device >= count)
+    return err(GPUAI_ERR_NO_DEVICE, "gpuai_searches_create: no such CUDA device");
+  gpuai_searches *s = new gpuai_searches;
+  s->device = device;
+  s->slots = max_searches;
+  s->pool_nodes = pool_nodes;
+  s->qmax = max_leaves_per_step;
+  s->ppl = playouts_per_leaf;
+  s->policy = policy;
+  s->seed = seed;
+  auto fail = [&](int rc) {
+    gpuai_searches_destroy(s);
+    return rc;
+  };
+  if (cudaSetDevice(device) != cudaSuccess) return fail(err(GPUAI_ERR_CUDA, "cudaSetDevice failed"));
+  cudaError_t e = cudaDeviceGetAttribute(&s->sms, cudaDevAttrMultiProcessorCount, device);
+  if (e == cudaSuccess) e = playout_occupancy(policy, kPlayoutBlock, &s->blocks_per_sm);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
+  const size_t P = pool_nodes, S = max_searches, L = (size_t)max_searches * max_leaves_per_step;
+  if (e == cudaSuccess) e = dalloc(s, &s->pool.board, P);
+  if (e == cudaSuccess) e = dalloc(s, &s->pool.parent, P);
+  if (e == cudaSuccess) e = dalloc(s, &s->pool.first_child, P);
+  if (e == cudaSuccess) e = dalloc(s, &s->pool.nchild, P);
+  if (e == cudaSuccess) e = dalloc(s, &s->pool.visits, P);
+  if (e == cudaSuccess) e = dalloc(s, &s->pool.score2, P);
+  if (e == cudaSuccess) e = dalloc(s, &s->pool.vloss, P);
+  if (e == cudaSuccess) e = dalloc(s, &s->pool.state, P);
+  if (e == cudaSuccess) e = dalloc(s, &s->pool.move, P);
+  if (e == cudaSuccess) e = dalloc(s, &s->pool.removed, P);
+  if (e == cudaSuccess) e = dalloc(s, &s->tab.root, S);
+  if (e == cudaSuccess) e = dalloc(s, &s->tab.node_next, S);
+  if (e == cudaSuccess) e = dalloc(s, &s->tab.node_end, S);
+  if (e == cudaSuccess) e = dalloc(s, &s->tab.stream_next, S);
+  if (e == cudaSuccess) e = dalloc(s, &s->tab.budget, S);
+  if (e == cudaSuccess) e = dalloc(s, &s->tab.done, S);
+  if (e == cudaSuccess) e = dalloc(s, &s->tab.quota_off, S + 1);
+  if (e == cudaSuccess) e = dalloc(s, &s->leaves.board, L);
+  if (e == cudaSuccess) e = dalloc(s, &s->leaves.node, L);
+  if (e == cudaSuccess) e = dalloc(s, &s->leaves.search, L);
+  if (e == cudaSuccess) e = dalloc(s, &s->leaves.stream, L);
+  if (e == cudaSuccess) e = dalloc(s, &s->leaves.out, L * playouts_per_leaf);
+  if (e == cudaSuccess) e = dalloc(s, &s->leaves.sizes, 2);
+  if (e == cudaSuccess) e = dalloc(s, &s->ctl, 4);
+  if (e == cudaSuccess) e = cudaMemsetAsync(s->tab.root, 0xff, S * sizeof(int32_t), s->stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(s->leaves.sizes, 0, 2 * sizeof(uint32_t), s->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+  if (e != cudaSuccess) return fail(cuda_err(e, "gpuai_searches_create"));
+  s->free_ranges[0] = pool_nodes;
+  s->start.assign(S, -1);
+  s->cap.assign(S, 0);
+  *out = s;
+  return GPUAI_OK;
+}
+
+void gpuai_searches_destroy(gpuai_searches *s) {
+  if (!s) return;
+  cudaSetDevice(s->device);
+  if (s->stream) cudaStreamSynchronize(s->stream);
+  if (s->graph) cudaGraphExecDestroy(s->graph);
+  for (void *p : s->allocations) cudaFree(p);
+  if (s->stream) cudaStreamDestroy(s->stream);
+  delete s;
+}
+
+int gpuai_searches_add(gpuai_searches *s, const gpuai_board *root, uint64_t playout_budget, uint32_t node_capacity,
+                       uint64_t stream_base, int32_t *slot) {
+  if (!s || !root || !slot) return err(GPUAI_ERR_INVALID, "gpuai_searches_add: NULL argument");
+  if (node_capacity < 1) return err(GPUAI_ERR_INVALID, "gpuai_searches_add: node_capacity must be >= 1");
+  if ((root->p1 & root->p2) || (root->kings & ~(root->p1 | root->p2)) || (root->meta & ~0xff01u))
+    return err(GPUAI_ERR_INVALID, "gpuai_searches_add: malformed board");
+  std::lock_guard<std::mutex> lock(s->mu);
+  int32_t free_slot = -1;
+  for (uint32_t i = 0; i < s->slots; i++)
+    if (s->start[i] < 0) {
+      free_slot = (int32_t)i;
+      break;
+    }
+  if (free_slot < 0) return err(GPUAI_ERR_OOM, "gpuai_searches_add: admission refused: all search slots busy");
+  auto it = s->free_ranges.begin();
+  for (; it != s->free_ranges.end(); ++it)
+    if (it->second >= node_capacity) break;
+  if (it == s->free_ranges.end())
+    return err(GPUAI_ERR_OOM, "gpuai_searches_add: admission refused: no free node range of that size");
+  const uint32_t start = it->first, len = it->second;
+  s->free_ranges.erase(it);
+  if (len > node_capacity) s->free_ranges[start + node_capacity] = len - node_capacity;
+  s->start[free_slot] = (int32_t)start;
+  s->cap[free_slot] = (int32_t)node_capacity;
+  SCK(cudaSetDevice(s->device), "cudaSetDevice");
+  init_search_kernel<<<1, 1, 0, s->stream>>>(s->pool, s->tab, free_slot, (int32_t)start, (int32_t)node_capacity,
+                                              make_uint4(root->p1, root->p2, root->kings, root->meta),
+                                              playout_budget, stream_base);
+  SCK(cudaGetLastError(), "init_search_kernel");
+  *slot = free_slot;
+  return GPUAI_OK;
+}
+
+int gpuai_searches_remove(gpuai_searches *s, int32_t slot) {
+  if (!s) return err(GPUAI_ERR_INVALID, "gpuai_searches_remove: NULL");
+  std::lock_guard<std::mutex> lock(s->mu);
+  if (slot < 0 || (uint32_t)slot >= s->slots || s->start[slot] < 0)
+    return err(GPUAI_ERR_INVALID, "gpuai_searches_remove: no such search");
+  SCK(cudaSetDevice(s->device), "cudaSetDevice");
+  remove_search_kernel<<<1, 1, 0, s->stream>>>(s->tab, slot);
+  SCK(cudaGetLastError(), "remove_search_kernel");
+  // return the node range, merging with free neighbours
+  uint32_t start = (uint32_t)s->start[slot], len = (uint32_t)s->cap[slot];
+  auto next = s->free_ranges.lower_bound(start);
+  if (next != s->free_ranges.end() && next->first == start + len) {
+    len += next->second;
+    next = s->free_ranges.erase(next);
+  }
+  if (next != s->free_ranges.begin()) {
+    auto prev = std::prev(next);
+    if (prev->first + prev->second == start) {
+      start = prev->first;
+      len += prev->second;
+      s->free_ranges.erase(prev);
+    }
+  }
+  s->free_ranges[start] = len;
+  s->start[slot] = -1;
+  s->cap[slot] = 0;
+  return GPUAI_OK;
+}
+
+int gpuai_searches_step(gpuai_searches *s, uint32_t steps, uint32_t leaves_per_search, int32_t use_graph) {
+  if (!s) return err(GPUAI_ERR_INVALID, "gpuai_searches_step: NULL");
+  if (leaves_per_search == 0 || leaves_per_search > s->qmax)
+    return err(GPUAI_ERR_INVALID, "gpuai_searches_step: leaves_per_search outside 1..max_leaves_per_step");
+  std::lock_guard<std::mutex> lock(s->mu);
+  SCK(cudaSetDevice(s->device), "cudaSetDevice");
+  if (!use_graph) {
+    for (uint32_t k = 0; k < steps; k++) {
+      const int rc = enqueue_step(s, leaves_per_search);
+      if (rc) return rc;
+    }
+    return GPUAI_OK;
+  }
+  if (!s->graph || s->graph_q != leaves_per_search) {
+    if (s->graph) cudaGraphExecDestroy(s->graph);
+    s->graph = nullptr;
+    cudaGraph_t g = nullptr;
+    SCK(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
+    const int rc = enqueue_step(s, leaves_per_search);
+    const cudaError_t e = cudaStreamEndCapture(s->stream, &g);
+    if (rc) {
+      if (g) cudaGraphDestroy(g);
+      return rc;
+    }
+    SCK(e, "end capture");
+    const cudaError_t ei = cudaGraphInstantiate(&s->graph, g, 0);
+    cudaGraphDestroy(g);
+    SCK(ei, "graph instantiate");
+    s->graph_q = leaves_per_search;
+  }
+  for (uint32_t k = 0; k < steps; k++) SCK(cudaGraphLaunch(s->graph, s->stream), "graph launch");
+  return GPUAI_OK;
+}
+
+int gpuai_searches_poll(gpuai_searches *s, uint64_t *done, uint64_t *budget, uint32_t n, uint32_t *status) {
+  if (!s || !done || !budget) return err(GPUAI_ERR_INVALID, "gpuai_searches_poll: NULL");
+  if (n > s->slots) return err(GPUAI_ERR_INVALID, "gpuai_searches_poll: n exceeds max_searches");
+  std::lock_guard<std::mutex> lock(s->mu);
+  SCK(cudaSetDevice(s->device), "cudaSetDevice");
+  uint32_t st = 0;
+  SCK(cudaMemcpyAsync(done, s->tab.done, n * sizeof(uint64_t), cudaMemcpyDeviceToHost, s->stream), "poll");
+  SCK(cudaMemcpyAsync(budget, s->tab.budget, n * sizeof(uint64_t), cudaMemcpyDeviceToHost, s->stream), "poll");
+  SCK(cudaMemcpyAsync(&st, s->ctl + 1, sizeof st, cudaMemcpyDeviceToHost, s->stream), "poll");
+  SCK(cudaStreamSynchronize(s->stream), "search steps");
+  for (uint32_t i = 0; i < n; i++)
+    if (s->start[i] < 0) done[i] = budget[i] = 0;
+  if (status) *status = st;
+  if (st) return err(GPUAI_ERR_LIMIT, "gpuai_searches_poll: a kernel reported a limit");
+  return GPUAI_OK;
+}
+
+int gpuai_searches_children(gpuai_searches *s, int32_t slot, gpuai_move *moves, uint32_t *visits,
+                            uint32_t *score2, uint32_t max_children, uint32_t *nchildren, uint32_t *nodes_used) {
+  if (!s || !nchildren) return err(GPUAI_ERR_INVALID, "gpuai_searches_children: NULL");
+  std::lock_guard<std::mutex> lock(s->mu);
+  if (slot < 0 || (uint32_t)slot >= s->slots || s->start[slot] < 0)
+    return err(GPUAI_ERR_INVALID, "gpuai_searches_children: no such search");
+  SCK(cudaSetDevice(s->device), "cudaSetDevice");
+  const int32_t r = s->start[slot];
+  int32_t first = -1, k = 0, next = 0;
+  uint4 rb;
+  SCK(cudaMemcpyAsync(&first, s->pool.first_child + r, 4, cudaMemcpyDeviceToHost, s->stream), "children");
+  SCK(cudaMemcpyAsync(&k, s->pool.nchild + r, 4, cudaMemcpyDeviceToHost, s->stream), "children");
+  SCK(cudaMemcpyAsync(&rb, s->pool.board + r, 16, cudaMemcpyDeviceToHost, s->stream), "children");
+  SCK(cudaMemcpyAsync(&next, s->tab.node_next + slot, 4, cudaMemcpyDeviceToHost, s->stream), "children");
+  SCK(cudaStreamSynchronize(s->stream), "children");
+  if (nodes_used) *nodes_used = (uint32_t)(next - r);
+  *nchildren = (uint32_t)k;
+  if (k <= 0) return GPUAI_OK;
+  std::vector<uint32_t> v(k), sc(k), mv(k), rm(k);
+  SCK(cudaMemcpyAsync(v.data(), s->pool.visits + first, 4 * k, cudaMemcpyDeviceToHost, s->stream), "children");
+  SCK(cudaMemcpyAsync(sc.data(), s->pool.score2 + first, 4 * k, cudaMemcpyDeviceToHost, s->stream), "children");
+  SCK(cudaMemcpyAsync(mv.data(), s->pool.move + first, 4 * k, cudaMemcpyDeviceToHost, s->stream), "children");
+  SCK(cudaMemcpyAsync(rm.data(), s->pool.removed + first, 4 * k, cudaMemcpyDeviceToHost, s->stream), "children");
+  SCK(cudaStreamSynchronize(s->stream), "children");
+  // full move records from the root's move list (same order as the children)
+  const Board b{rb.x, rb.y, rb.z, rb.w};
+  Side sd;
+  make_side(b, sd);
+  std::vector<gpuai_move> all;
+  for_each_move(sd, jumpers(sd), [&](int from, int to, uint32_t, int jumps, uint32_t dirs) {
+    uint32_t w[8];
+    pack_move(b, from, to, jumps, dirs, w);
+    gpuai_move m;
+    std::memcpy(&m, w, sizeof m);
+    all.push_back(m);
+    return false;
+  });
+  for (uint32_t i = 0; i < (uint32_t)k && i < max_children; i++) {
+    if (visits) visits[i] = v[i];
+    if (score2) score2[i] = sc[i];
+    if (moves && i < all.size()) moves[i] = all[i];
+  }
+  return GPUAI_OK;
+}
+
+}  // extern "C"

@@ -80,8 +80,20 @@ def load_library(path: str = LIB_PATH):
     lib.gpuai_device_info.argtypes = [ctypes.c_void_p, _i32p, _i32p, _i32p]
     lib.gpuai_set_launch.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32]
     lib.gpuai_get_launch.argtypes = [ctypes.c_void_p, ctypes.c_int32, _i32p, _i32p, _i32p]
+    lib.gpuai_searches_create.argtypes = [ctypes.c_int, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
+                                          ctypes.c_uint32, ctypes.c_int32, ctypes.c_uint64,
+                                          ctypes.POINTER(ctypes.c_void_p)]
+    lib.gpuai_searches_destroy.argtypes = [ctypes.c_void_p]
+    lib.gpuai_searches_destroy.restype = None
+    lib.gpuai_searches_add.argtypes = [ctypes.c_void_p, _u32p, ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint64,
+                                       _i32p]
+    lib.gpuai_searches_remove.argtypes = [ctypes.c_void_p, ctypes.c_int32]
+    lib.gpuai_searches_step.argtypes = [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_int32]
+    lib.gpuai_searches_poll.argtypes = [ctypes.c_void_p, _u64p, _u64p, ctypes.c_uint32, _u32p]
+    lib.gpuai_searches_children.argtypes = [ctypes.c_void_p, ctypes.c_int32, _u8p, _u32p, _u32p, ctypes.c_uint32,
+                                            _u32p, _u32p]
     for name in header_symbols():
-        if name not in ("gpuai_last_error", "gpuai_destroy"):
+        if name not in ("gpuai_last_error", "gpuai_destroy", "gpuai_searches_destroy"):
             getattr(lib, name).restype = ctypes.c_int
     _lib = lib
     return lib
@@ -184,3 +196,74 @@ class Engine:
         a, b, c = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
         _check(self.lib.gpuai_device_info(self.ctx, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
         return {"sms": a.value, "blocks_per_sm": b.value, "block_threads": c.value}
+
+
+class Searches:
+    """Many MCTS searches with device-resident trees (gpuai_searches_*)."""
+
+    def __init__(self, max_searches: int, pool_nodes: int, max_leaves_per_step: int = 64,
+                 playouts_per_leaf: int = 1, policy: int = POLICY_RANDOM, seed: int = 0, device: int = 0):
+        self.lib = load_library()
+        h = ctypes.c_void_p()
+        _check(self.lib.gpuai_searches_create(device, max_searches, pool_nodes, max_leaves_per_step,
+                                              playouts_per_leaf, policy, seed, ctypes.byref(h)))
+        self.h = h
+        self.max_searches = max_searches
+
+    def close(self):
+        if self.h:
+            self.lib.gpuai_searches_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def add(self, root, budget: int, node_capacity: int, stream_base: int) -> int:
+        b = np.ascontiguousarray(root, dtype=np.uint32).reshape(4)
+        slot = ctypes.c_int32()
+        _check(self.lib.gpuai_searches_add(self.h, b.ctypes.data_as(_u32p), budget, node_capacity, stream_base,
+                                           ctypes.byref(slot)))
+        return slot.value
+
+    def try_add(self, root, budget: int, node_capacity: int, stream_base: int):
+        """Slot, or None when admission is refused (no slot / node range free)."""
+        try:
+            return self.add(root, budget, node_capacity, stream_base)
+        except GpuAIError as e:
+            if e.code == ERR_OOM:
+                return None
+            raise
+
+    def remove(self, slot: int):
+        _check(self.lib.gpuai_searches_remove(self.h, slot))
+
+    def step(self, steps: int, leaves_per_search: int, use_graph: bool = True):
+        _check(self.lib.gpuai_searches_step(self.h, steps, leaves_per_search, 1 if use_graph else 0))
+
+    def poll(self):
+        done = np.zeros(self.max_searches, np.uint64)
+        budget = np.zeros(self.max_searches, np.uint64)
+        st = ctypes.c_uint32()
+        _check(self.lib.gpuai_searches_poll(self.h, done.ctypes.data_as(_u64p), budget.ctypes.data_as(_u64p),
+                                            self.max_searches, ctypes.byref(st)))
+        return done, budget
+
+    def children(self, slot: int, max_children: int = 64):
+        moves = np.zeros((max_children, 32), np.uint8)
+        visits = np.zeros(max_children, np.uint32)
+        score2 = np.zeros(max_children, np.uint32)
+        n = ctypes.c_uint32()
+        used = ctypes.c_uint32()
+        _check(self.lib.gpuai_searches_children(self.h, slot, moves.ctypes.data_as(_u8p), visits.ctypes.data_as(_u32p),
+                                                score2.ctypes.data_as(_u32p), max_children, ctypes.byref(n),
+                                                ctypes.byref(used)))
+        k = min(n.value, max_children)
+        return {"moves": moves[:k], "visits": visits[:k], "score2": score2[:k], "nodes": used.value}
+
+    def best(self, slot: int):
+        c = self.children(slot)
+        i = int(np.argmax(c["visits"]))
+        return c["moves"][i], c

@@ -114,6 +114,38 @@ int gpuai_set_launch(gpuai_ctx *ctx, int32_t policy, int32_t block_threads, int3
 int gpuai_get_launch(gpuai_ctx *ctx, int32_t policy, int32_t *block_threads, int32_t *blocks_per_sm,
                      int32_t *max_blocks_per_sm);
 
+/* ---- many searches with device-resident trees ----
+ * Replaces the reference's one-search-per-MCTSPlayer loop
+ * (src/player.cpp:134-150, src/mcts.cpp:63-191) with searches whose UCT trees
+ * live in one node pool in device memory.  One step advances every active
+ * search: up to `leaves_per_search` UCT descents with virtual loss per search
+ * (leaves expanded the second time they are reached), playouts_per_leaf GPU
+ * playouts per leaf, and backpropagation; the step's four kernels can be
+ * replayed as a CUDA graph.  A search's result does not depend on the other
+ * searches it shares steps with.  Best move = most visited root child. */
+typedef struct gpuai_searches gpuai_searches;
+
+/* pool_nodes: node capacity of the shared pool (52 bytes of device memory per
+ * node); max_leaves_per_step bounds leaves_per_search. */
+int gpuai_searches_create(int device, uint32_t max_searches, uint32_t pool_nodes, uint32_t max_leaves_per_step,
+                          uint32_t playouts_per_leaf, int32_t policy, uint64_t seed, gpuai_searches **out);
+void gpuai_searches_destroy(gpuai_searches *s);
+/* Admit a search from `root` that stops after `playout_budget` playouts and
+ * may grow to `node_capacity` nodes; its playouts use random stream ids from
+ * stream_base on.  GPUAI_ERR_OOM = admission refused (no free slot or no free
+ * node range of that size). */
+int gpuai_searches_add(gpuai_searches *s, const gpuai_board *root, uint64_t playout_budget, uint32_t node_capacity,
+                       uint64_t stream_base, int32_t *slot);
+int gpuai_searches_remove(gpuai_searches *s, int32_t slot);
+/* Enqueue `steps` steps (no synchronisation). */
+int gpuai_searches_step(gpuai_searches *s, uint32_t steps, uint32_t leaves_per_search, int32_t use_graph);
+/* Synchronise; playouts done and budget of slots 0..n-1 (0 for free slots). */
+int gpuai_searches_poll(gpuai_searches *s, uint64_t *done, uint64_t *budget, uint32_t n, uint32_t *status);
+/* Root children of a search: moves (reference move-list order), visits and
+ * score in half points for the player to move at the root. */
+int gpuai_searches_children(gpuai_searches *s, int32_t slot, gpuai_move *moves, uint32_t *visits,
+                            uint32_t *score2, uint32_t max_children, uint32_t *nchildren, uint32_t *nodes_used);
+
 /* Playouts that allocate no device memory, for callers that may not call
  * cudaMalloc: for example a search server that reserves the whole device
  * memory budget for its trees up front, or a move loop with a hard per-move
