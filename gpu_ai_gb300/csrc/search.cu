@@ -320,10 +320,12 @@ cudaError_t dalloc(gpuai_searches *s, T **p, size_t n) {
 
 int enqueue_step(gpuai_searches *s, uint32_t q) {
   const cudaStream_t st = s->stream;
+  // work counter and ply count restart every step; status bits accumulate
+  // until poll reads them
+  SCK(cudaMemsetAsync(s->ctl, 0, sizeof(uint32_t), st), "reset work counter");
   quota_kernel<<<1, 1024, 0, st>>>(s->tab, s->slots, q, s->ppl, s->leaves);
   const uint32_t sel_threads = s->slots * 32u;
   select_kernel<<<(sel_threads + 255) / 256, 256, 0, st>>>(s->pool, s->tab, s->leaves, s->slots, s->ppl, s->ctl + 1);
-  SCK(cudaMemsetAsync(s->ctl, 0, 4 * sizeof(uint32_t), st), "reset work counter");
   PlayoutArgs a;
   a.pos = reinterpret_cast<const Board *>(s->leaves.board);
   a.offsets = nullptr;
@@ -404,6 +406,7 @@ int gpuai_searches_create(int device, uint32_t max_searches, uint32_t pool_nodes
   if (e == cudaSuccess) e = dalloc(s, &s->ctl, 4);
   if (e == cudaSuccess) e = cudaMemsetAsync(s->tab.root, 0xff, S * sizeof(int32_t), s->stream);
   if (e == cudaSuccess) e = cudaMemsetAsync(s->leaves.sizes, 0, 2 * sizeof(uint32_t), s->stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(s->ctl, 0, 4 * sizeof(uint32_t), s->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
   if (e != cudaSuccess) return fail(cuda_err(e, "gpuai_searches_create"));
   s->free_ranges[0] = pool_nodes;
@@ -529,6 +532,7 @@ int gpuai_searches_poll(gpuai_searches *s, uint64_t *done, uint64_t *budget, uin
   SCK(cudaMemcpyAsync(budget, s->tab.budget, n * sizeof(uint64_t), cudaMemcpyDeviceToHost, s->stream), "poll");
   SCK(cudaMemcpyAsync(&st, s->ctl + 1, sizeof st, cudaMemcpyDeviceToHost, s->stream), "poll");
   SCK(cudaStreamSynchronize(s->stream), "search steps");
+  if (st) SCK(cudaMemsetAsync(s->ctl + 1, 0, sizeof(uint32_t), s->stream), "clear status");  // reported once
   for (uint32_t i = 0; i < n; i++)
     if (s->start[i] < 0) done[i] = budget[i] = 0;
   if (status) *status = st;
