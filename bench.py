@@ -324,6 +324,52 @@ def run_ours(args):
     print(json.dumps(line), flush=True)
 
 
+def run_searches(args):
+    """Batched searches with device-resident trees: 2,048 games at U{0..60}
+    random plies, playout budgets lognormal clipped to [1K, 256K], all advanced
+    together; total playouts/s with graph-replayed steps and with eager
+    launches."""
+    import torch
+    from gpu_ai_gb300 import Engine, Searches
+
+    n_games, q, ppl = args.games, args.leaves, args.playouts_per_leaf
+    eng = Engine(0)
+    roots = eng.random_positions(4242, n_games, 0, 60)
+    rng = np.random.default_rng(4242)
+    budgets = np.clip(np.exp(rng.normal(np.log(16384), 1.2, n_games)), 1024, 262144).astype(np.int64)
+    budgets = (budgets + ppl - 1) // ppl * ppl
+    caps = np.minimum(budgets, 131072).astype(np.int64) * 2
+    result = {}
+    for mode in ("graph", "eager"):
+        s = Searches(n_games, int(caps.sum()) + 1024, q, playouts_per_leaf=ppl)
+        for i in range(n_games):
+            s.add(roots[i], int(budgets[i]), int(caps[i]), i << 40)
+        torch.cuda.synchronize()
+        steps = 0
+        t0 = time.perf_counter()
+        while True:
+            done, budget = s.poll()
+            if (done >= budget).all():
+                break
+            s.step(8, q, mode == "graph")
+            steps += 8
+        el = time.perf_counter() - t0
+        total = int(done.sum())
+        result[mode] = {"seconds": el, "steps": steps, "playouts": total, "playouts_per_s": total / el}
+        s.close()
+    g, e = result["graph"], result["eager"]
+    line = {
+        "metric": "checkers playouts/sec, batched searches with device-resident trees", "value": g["playouts_per_s"],
+        "unit": UNIT, "n_gpus": 1, "higher_is_better": True, "dtype": "u32", "data": "synthetic (seeded positions)",
+        "config": {"workload": f"{n_games} games at 0-60 random plies, budgets lognormal in [1K, 256K]",
+                   "leaves_per_search_per_step": q, "playouts_per_leaf": ppl,
+                   "total_budget": int(budgets.sum())},
+        "graph": g, "eager": e,
+        "launch_overhead_us_per_step": (e["seconds"] - g["seconds"]) / max(1, g["steps"]) * 1e6,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -333,11 +379,17 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--block", type=int, default=0, help="threads per block of the playout kernel (0: default)")
     ap.add_argument("--blocks-per-sm", type=int, default=0, help="resident blocks per SM (0: as many as fit)")
+    ap.add_argument("--workload", choices=["playouts", "searches"], default="playouts")
+    ap.add_argument("--games", type=int, default=2048, help="searches workload: number of games")
+    ap.add_argument("--leaves", type=int, default=64, help="searches workload: leaves per search per step")
+    ap.add_argument("--playouts-per-leaf", type=int, default=8, help="searches workload: playouts per leaf")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "searches":
+        run_searches(args)
     else:
         run_ours(args)
 
