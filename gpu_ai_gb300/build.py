@@ -26,7 +26,7 @@ INCLUDE = os.path.join(ROOT, "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O3",
-              "-I" + INCLUDE] + ARCH
+              "-I" + INCLUDE, "-I" + CSRC] + ARCH
 CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-Wall", "-Wextra", "-pthread", "-I" + INCLUDE, "-I" + CSRC]
 
 CUDA_UNITS = ["kernels.cu", "capi.cu", "noalloc.cu", "search.cu"]

@@ -8,10 +8,13 @@
 //
 //   quota_kernel     leaf slots per search this step (min(Q, remaining
 //                    budget)), prefix sums, total leaves / playouts
-//   select_kernel    one warp per search: Q sequential UCT descents with
-//                    virtual loss, expanding a leaf (all children at once)
-//                    the second time it is reached; writes leaf boards and
-//                    per-leaf random-stream ids
+//   select_kernel    one warp per search: the step's Q leaf slots are split
+//                    over the tree level by level the way the reference's
+//                    GameTree::select splits a batch (src/mcts.cpp:63-157):
+//                    untried children share the slots equally, otherwise in
+//                    proportion to UCB1, remainders to the heaviest children;
+//                    a leaf given more than one slot is expanded; the lanes
+//                    of the warp take one frontier node each
 //   playout_kernel   the playout kernel on the leaf boards (sizes and stream
 //                    ids read from device memory)
 //   backprop_kernel  one thread per leaf: visits and score up the path,
@@ -21,7 +24,12 @@
 // search is selected by a single warp in a fixed order and its playouts use
 // its own stream ids, a search's tree and result do not depend on which other
 // searches share the steps.
+//
+// Node record (one uint4 per node, read with one load): x = first child (-1
+// before expansion), y = number of children | state << 16, z = playouts through
+// the node, w = score in half points of the player who moved into the node.
 #include "../../include/gpuai.h"
+#include "host/state.hpp"
 #include "launch.h"
 #include "rules.cuh"
 
@@ -42,12 +50,16 @@ namespace {
 constexpr uint32_t kExpanded = 1u, kTerminal = 2u;
 constexpr int kMaxSelectDepth = 512;
 constexpr uint32_t kStatusSelectDepth = 8u;
+constexpr uint32_t kSelectWarps = 4;   // searches per select block
+constexpr uint32_t kMaxLeavesPerStep = 256;  // frontier capacity per search
 constexpr float kUcbC = 1.41421356f;
+constexpr int kMaxChildren = 64;  // moves per position handled by split_slots
 
 struct Pool {  // one entry per node
+  uint4 *info;   // {first child, nchild | state << 16, visits, score2}
   uint4 *board;
-  int32_t *parent, *first_child, *nchild;
-  uint32_t *visits, *score2, *vloss, *state, *move, *removed;
+  int32_t *parent;
+  uint32_t *move, *removed;
 };
 
 struct Table {  // one entry per search slot
@@ -117,110 +129,197 @@ __global__ void __launch_bounds__(1024) quota_kernel(Table t, uint32_t slots, ui
   }
 }
 
-// Creates all children of node n (lane 0 writes, the warp waits); false when
-// the search's node range is full.
-__device__ bool expand(const Pool &p, const Table &t, uint32_t s, int32_t n, uint32_t lane) {
-  int ok = 0;
-  if (lane == 0) {
-    const uint4 bv = p.board[n];
-    const Board b{bv.x, bv.y, bv.z, bv.w};
-    Side sd;
-    make_side(b, sd);
-    const uint32_t J = jumpers(sd);
-    const int k = count_moves(sd, J);
-    const int32_t base = t.node_next[s];
-    if (k > 0 && base + k <= t.node_end[s]) {
-      t.node_next[s] = base + k;
-      int32_t c = base;
-      for_each_move(sd, J, [&](int from, int to, uint32_t removed, int jumps, uint32_t) {
-        Board cb = b;
-        apply_move(cb, from, to, removed);
-        p.board[c] = make_uint4(cb.p1, cb.p2, cb.kings, cb.meta);
-        p.parent[c] = n;
-        p.first_child[c] = -1;
-        p.nchild[c] = 0;
-        p.visits[c] = 0;
-        p.score2[c] = 0;
-        p.vloss[c] = 0;
-        p.state[c] = board_terminal(cb) ? kTerminal : 0u;
-        p.move[c] = (uint32_t)from | ((uint32_t)to << 8) | ((uint32_t)jumps << 16) |
-                    ((promotes(b, from, to) ? 1u : 0u) << 24);
-        p.removed[c] = removed;
-        c++;
-        return false;
-      });
-      p.first_child[n] = base;
-      p.nchild[n] = k;
-      p.state[n] |= kExpanded;
-      ok = 1;
-    }
-  }
-  ok = __shfl_sync(0xffffffffu, ok, 0);
-  __syncwarp();
-  return ok != 0;
+// Number of children node n would get (its legal moves), 0 for none.
+__device__ int child_count(const Pool &p, int32_t n) {
+  const uint4 bv = p.board[n];
+  const Board b{bv.x, bv.y, bv.z, bv.w};
+  Side sd;
+  make_side(b, sd);
+  const int k = count_moves(sd, jumpers(sd));
+  return (k > 0 && k <= kMaxChildren) ? k : 0;
 }
 
-// One warp per search: Q sequential descents with virtual loss.
-__global__ void __launch_bounds__(256) select_kernel(Pool p, Table t, Leaves l, uint32_t slots, uint32_t ppl,
-                                                     uint32_t *status) {
-  const uint32_t lane = threadIdx.x & 31u;
-  const uint32_t s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+// Writes the k children of node n at node indices base.. (called by one lane).
+__device__ void expand_at(const Pool &p, int32_t n, int32_t base, int k) {
+  const uint4 bv = p.board[n];
+  const Board b{bv.x, bv.y, bv.z, bv.w};
+  Side sd;
+  make_side(b, sd);
+  int32_t c = base;
+  for_each_move(sd, jumpers(sd), [&](int from, int to, uint32_t removed, int jumps, uint32_t) {
+    Board cb = b;
+    apply_move(cb, from, to, removed);
+    p.board[c] = make_uint4(cb.p1, cb.p2, cb.kings, cb.meta);
+    p.parent[c] = n;
+    p.info[c] = make_uint4(0xffffffffu, (board_terminal(cb) ? kTerminal : 0u) << 16, 0u, 0u);
+    p.move[c] = (uint32_t)from | ((uint32_t)to << 8) | ((uint32_t)jumps << 16) |
+                ((promotes(b, from, to) ? 1u : 0u) << 24);
+    p.removed[c] = removed;
+    c++;
+    return false;
+  });
+  const uint4 inf = p.info[n];
+  p.info[n] = make_uint4((uint32_t)base, (uint32_t)k | (((inf.y >> 16) | kExpanded) << 16), inf.z, inf.w);
+}
+
+// Splits T slots over the children of node n (the reference's rule,
+// src/mcts.cpp:95-136): untried children share them equally; otherwise in
+// proportion to UCB1 weights rounded down; the remainder goes one each to the
+// heaviest children (first on ties).  Weights that sum to zero count as
+// equal.  Calls emit(child, slots) for children given slots, in child order.
+template <class Emit>
+__device__ void split_slots(const Pool &p, int32_t first, int k, uint32_t parent_visits, uint32_t T, Emit &&emit) {
+  const float lnN = logf((float)(parent_visits > 0 ? parent_visits : 1u));
+  float wsum = 0.0f;
+  int untried = 0;
+  for (int c = 0; c < k; c++) {
+    const uint4 ci = p.info[first + c];
+    if (ci.z == 0) untried++;
+    else wsum += 0.5f * (float)ci.w / (float)ci.z + kUcbC * sqrtf(lnN / (float)ci.z);
+  }
+  const bool equal = untried == 0 && !(wsum > 0.0f);
+  uint32_t assigned = 0;
+  uint32_t give[kMaxChildren];
+  float w[kMaxChildren];
+  for (int c = 0; c < k; c++) {
+    const uint4 ci = p.info[first + c];
+    w[c] = ci.z == 0 ? 3.0e38f : (equal ? 1.0f : 0.5f * (float)ci.w / (float)ci.z + kUcbC * sqrtf(lnN / (float)ci.z));
+    if (untried > 0) give[c] = ci.z == 0 ? T / (uint32_t)untried : 0u;
+    else give[c] = (uint32_t)((float)T * (w[c] / (equal ? (float)k : wsum)));
+    assigned += give[c];
+  }
+  uint64_t extra = 0;  // children that already took one of the remaining slots
+  while (assigned < T) {
+    float mw = -1.0f;
+    int opt = -1;
+    for (int c = 0; c < k; c++)
+      if (!((extra >> c) & 1ull) && w[c] > mw) {
+        mw = w[c];
+        opt = c;
+      }
+    if (opt < 0) break;  // cannot happen: fewer than k slots remain
+    extra |= 1ull << opt;
+    give[opt]++;
+    assigned++;
+  }
+  for (int c = 0; c < k; c++)
+    if (give[c]) emit(first + c, give[c]);
+}
+
+// One warp per search.  The frontier holds (node, slots) pairs; each round
+// every lane takes frontier entries, expands or splits them, and the warp
+// compacts the children it produced into the next frontier and the leaf
+// slots it produced into the search's output range.
+__global__ void __launch_bounds__(32 * kSelectWarps) select_kernel(Pool p, Table t, Leaves l, uint32_t slots,
+                                                                   uint32_t ppl, uint32_t *status) {
+  __shared__ int32_t f_node[kSelectWarps][2][kMaxLeavesPerStep];
+  __shared__ uint32_t f_cnt[kSelectWarps][2][kMaxLeavesPerStep];
+  const uint32_t lane = threadIdx.x & 31u, wi = threadIdx.x >> 5;
+  const uint32_t s = blockIdx.x * kSelectWarps + wi;
   if (s >= slots) return;
   const int32_t root = t.root[s];
   if (root < 0) return;
   const uint32_t off = t.quota_off[s], q = t.quota_off[s + 1] - off;
-  for (uint32_t i = 0; i < q; i++) {
-    int32_t n = root;
-    for (int depth = 0;; depth++) {
-      const uint32_t st = p.state[n];
-      if (st & kTerminal) break;
-      if (!(st & kExpanded)) {
-        if (n != root && p.visits[n] == 0) break;  // a fresh leaf plays out first
-        if (!expand(p, t, s, n, lane)) break;     // node range full: play out from n
-      }
-      if (depth >= kMaxSelectDepth) {
-        if (lane == 0) atomicOr(status, kStatusSelectDepth);
-        break;
-      }
-      // UCB1 with virtual loss over the children; first best on ties
-      const int32_t first = p.first_child[n], k = p.nchild[n];
-      uint32_t tot = 0;
-      for (int32_t c = (int32_t)lane; c < k; c += 32) tot += p.visits[first + c] + p.vloss[first + c];
-      for (int o = 16; o > 0; o >>= 1) tot += __shfl_xor_sync(0xffffffffu, tot, o);
-      const float lnN = logf((float)tot + 1.0f);
-      float best = -1.0f;
-      int32_t bi = 0x7fffffff;
-      for (int32_t c = (int32_t)lane; c < k; c += 32) {
-        const uint32_t d = p.visits[first + c] + p.vloss[first + c];
-        const float v = d == 0 ? 3.0e38f
-                               : 0.5f * (float)p.score2[first + c] / (float)d + kUcbC * sqrtf(lnN / (float)d);
-        if (v > best) {
-          best = v;
-          bi = c;
+  if (q == 0) return;
+  int cur = 0;
+  uint32_t nf = 1, emitted = 0;
+  int32_t node_next = t.node_next[s];
+  const int32_t node_end = t.node_end[s];
+  if (lane == 0) {
+    f_node[wi][0][0] = root;
+    f_cnt[wi][0][0] = q;
+  }
+  __syncwarp();
+  for (int depth = 0; nf > 0; depth++) {
+    if (depth >= kMaxSelectDepth) {
+      if (lane == 0) atomicOr(status, kStatusSelectDepth);
+      break;
+    }
+    uint32_t next_n = 0;
+    for (uint32_t base = 0; base < nf; base += 32) {
+      const uint32_t e = base + lane;
+      // pass 1: what each lane's entry produces (children entries or leaf slots)
+      int32_t n = -1, first = 0, k = 0;
+      uint32_t T = 0, leaf = 0, kids = 0, visits = 0, st = 0;
+      int grow = 0;  // children this lane's node gets if it is expanded now
+      if (e < nf) {
+        n = f_node[wi][cur][e];
+        T = f_cnt[wi][cur][e];
+        const uint4 inf = p.info[n];
+        st = inf.y >> 16;
+        visits = inf.z;
+        first = (int32_t)inf.x;
+        k = (int32_t)(inf.y & 0xffffu);
+        if (st & kTerminal) leaf = T;
+        else if (!(st & kExpanded)) {
+          if (T == 1) leaf = 1;
+          else grow = child_count(p, n);
+          if (T > 1 && grow == 0) leaf = T;
         }
       }
-      for (int o = 16; o > 0; o >>= 1) {
-        const float ov = __shfl_xor_sync(0xffffffffu, best, o);
-        const int32_t oi = __shfl_xor_sync(0xffffffffu, bi, o);
-        if (ov > best || (ov == best && oi < bi)) {
-          best = ov;
-          bi = oi;
+      // node indices for this round's expansions, in lane order; an expansion
+      // that does not fit the search's node range plays out instead
+      uint32_t gx = (uint32_t)grow;
+      for (uint32_t o = 1; o < 32; o <<= 1) {
+        const uint32_t a = __shfl_up_sync(0xffffffffu, gx, o);
+        if (lane >= o) gx += a;
+      }
+      const bool fits = grow > 0 && node_next + (int32_t)gx <= node_end;
+      const uint32_t fit_end = __reduce_max_sync(0xffffffffu, fits ? gx : 0u);
+      if (fits) {
+        first = node_next + (int32_t)gx - grow;
+        k = grow;
+        expand_at(p, n, first, k);
+      } else if (grow > 0) {
+        leaf = T;
+      }
+      node_next += (int32_t)fit_end;
+      if (e < nf) {
+        if (!leaf) split_slots(p, first, k, visits, T, [&](int32_t, uint32_t) { kids++; });
+      }
+      __syncwarp();
+      // warp prefix sums of children entries and leaf slots
+      uint32_t kx = kids, lx = leaf;
+      for (uint32_t o = 1; o < 32; o <<= 1) {
+        const uint32_t a = __shfl_up_sync(0xffffffffu, kx, o), b2 = __shfl_up_sync(0xffffffffu, lx, o);
+        if (lane >= o) {
+          kx += a;
+          lx += b2;
         }
       }
-      n = first + bi;
-      if (lane == 0) p.vloss[n] += 1u;
+      const uint32_t kid_at = next_n + kx - kids, leaf_at = emitted + lx - leaf;
+      next_n += __shfl_sync(0xffffffffu, kx, 31);
+      emitted += __shfl_sync(0xffffffffu, lx, 31);
+      // pass 2: write children entries and leaf slots
+      if (e < nf) {
+        if (leaf) {
+          const uint4 bv = p.board[n];
+          for (uint32_t r = 0; r < leaf; r++) {
+            const uint32_t o = off + leaf_at + r;
+            l.board[o] = bv;
+            l.node[o] = n;
+            l.search[o] = (int32_t)s;
+          }
+        } else {
+          uint32_t w = kid_at;
+          split_slots(p, first, k, visits, T, [&](int32_t child, uint32_t cnt) {
+            f_node[wi][cur ^ 1][w] = child;
+            f_cnt[wi][cur ^ 1][w] = cnt;
+            w++;
+          });
+        }
+      }
       __syncwarp();
     }
-    if (lane == 0) {
-      const uint32_t o = off + i;
-      l.board[o] = p.board[n];
-      l.node[o] = n;
-      l.search[o] = (int32_t)s;
-      l.stream[o] = t.stream_next[s];
-      t.stream_next[s] += ppl;
-    }
-    __syncwarp();
+    cur ^= 1;
+    nf = next_n;
   }
+  if (lane == 0) t.node_next[s] = node_next;
+  // per-slot random streams, in slot order
+  const unsigned long long sbase = t.stream_next[s];
+  for (uint32_t i = lane; i < q; i += 32) l.stream[off + i] = sbase + (unsigned long long)i * ppl;
+  __syncwarp();
+  if (lane == 0) t.stream_next[s] = sbase + (unsigned long long)q * ppl;
 }
 
 // One thread per leaf: outcomes up the path (score in half points for the
@@ -239,10 +338,10 @@ __global__ void backprop_kernel(Pool p, Table t, Leaves l, uint32_t ppl, uint32_
   }
   for (int32_t n = l.node[i]; n >= 0; n = p.parent[n]) {
     const uint32_t mover = (p.board[n].w & 1u) ^ 1u;  // 0: PLAYER_1 moved into n
-    atomicAdd(&p.visits[n], ppl);
-    atomicAdd(&p.score2[n], 2u * (mover == 0 ? w1 : w2) + dr);
-    if (n != root) atomicSub(&p.vloss[n], 1u);
+    atomicAdd(&p.info[n].z, ppl);
+    atomicAdd(&p.info[n].w, 2u * (mover == 0 ? w1 : w2) + dr);
   }
+  (void)root;
   atomicAdd(&t.done[s], (unsigned long long)ppl);
 }
 
@@ -250,13 +349,8 @@ __global__ void init_search_kernel(Pool p, Table t, int32_t slot, int32_t start,
                                    unsigned long long budget, unsigned long long stream_base) {
   p.board[start] = board;
   p.parent[start] = -1;
-  p.first_child[start] = -1;
-  p.nchild[start] = 0;
-  p.visits[start] = 0;
-  p.score2[start] = 0;
-  p.vloss[start] = 0;
   const Board b{board.x, board.y, board.z, board.w};
-  p.state[start] = board_terminal(b) ? kTerminal : 0u;
+  p.info[start] = make_uint4(0xffffffffu, (board_terminal(b) ? kTerminal : 0u) << 16, 0u, 0u);
   p.move[start] = 0;
   p.removed[start] = 0;
   t.root[slot] = start;
@@ -324,8 +418,8 @@ int enqueue_step(gpuai_searches *s, uint32_t q) {
   // until poll reads them
   SCK(cudaMemsetAsync(s->ctl, 0, sizeof(uint32_t), st), "reset work counter");
   quota_kernel<<<1, 1024, 0, st>>>(s->tab, s->slots, q, s->ppl, s->leaves);
-  const uint32_t sel_threads = s->slots * 32u;
-  select_kernel<<<(sel_threads + 255) / 256, 256, 0, st>>>(s->pool, s->tab, s->leaves, s->slots, s->ppl, s->ctl + 1);
+  select_kernel<<<(s->slots + kSelectWarps - 1) / kSelectWarps, 32 * kSelectWarps, 0, st>>>(
+      s->pool, s->tab, s->leaves, s->slots, s->ppl, s->ctl + 1);
   PlayoutArgs a;
   a.pos = reinterpret_cast<const Board *>(s->leaves.board);
   a.offsets = nullptr;
@@ -358,6 +452,8 @@ int gpuai_searches_create(int device, uint32_t max_searches, uint32_t pool_nodes
   if (max_searches == 0 || pool_nodes == 0 || max_leaves_per_step == 0 || playouts_per_leaf == 0)
     return err(GPUAI_ERR_INVALID, "gpuai_searches_create: zero size");
   if (policy < 0 || policy > 2) return err(GPUAI_ERR_INVALID, "gpuai_searches_create: unknown policy");
+  if (max_leaves_per_step > kMaxLeavesPerStep)
+    return err(GPUAI_ERR_INVALID, "gpuai_searches_create: max_leaves_per_step above 256");
   if ((uint64_t)max_searches * max_leaves_per_step * playouts_per_leaf > 0x7fffffffull || pool_nodes > 0x7fffffffu)
     return err(GPUAI_ERR_INVALID, "gpuai_searches_create: sizes exceed 2^31");
   int count = 0;
@@ -380,14 +476,9 @@ int gpuai_searches_create(int device, uint32_t max_searches, uint32_t pool_nodes
   if (e == cudaSuccess) e = playout_occupancy(policy, kPlayoutBlock, &s->blocks_per_sm);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
   const size_t P = pool_nodes, S = max_searches, L = (size_t)max_searches * max_leaves_per_step;
+  if (e == cudaSuccess) e = dalloc(s, &s->pool.info, P);
   if (e == cudaSuccess) e = dalloc(s, &s->pool.board, P);
   if (e == cudaSuccess) e = dalloc(s, &s->pool.parent, P);
-  if (e == cudaSuccess) e = dalloc(s, &s->pool.first_child, P);
-  if (e == cudaSuccess) e = dalloc(s, &s->pool.nchild, P);
-  if (e == cudaSuccess) e = dalloc(s, &s->pool.visits, P);
-  if (e == cudaSuccess) e = dalloc(s, &s->pool.score2, P);
-  if (e == cudaSuccess) e = dalloc(s, &s->pool.vloss, P);
-  if (e == cudaSuccess) e = dalloc(s, &s->pool.state, P);
   if (e == cudaSuccess) e = dalloc(s, &s->pool.move, P);
   if (e == cudaSuccess) e = dalloc(s, &s->pool.removed, P);
   if (e == cudaSuccess) e = dalloc(s, &s->tab.root, S);
@@ -548,35 +639,31 @@ int gpuai_searches_children(gpuai_searches *s, int32_t slot, gpuai_move *moves, 
     return err(GPUAI_ERR_INVALID, "gpuai_searches_children: no such search");
   SCK(cudaSetDevice(s->device), "cudaSetDevice");
   const int32_t r = s->start[slot];
-  int32_t first = -1, k = 0, next = 0;
-  uint4 rb;
-  SCK(cudaMemcpyAsync(&first, s->pool.first_child + r, 4, cudaMemcpyDeviceToHost, s->stream), "children");
-  SCK(cudaMemcpyAsync(&k, s->pool.nchild + r, 4, cudaMemcpyDeviceToHost, s->stream), "children");
+  int32_t next = 0;
+  uint4 rb, ri;
+  SCK(cudaMemcpyAsync(&ri, s->pool.info + r, 16, cudaMemcpyDeviceToHost, s->stream), "children");
   SCK(cudaMemcpyAsync(&rb, s->pool.board + r, 16, cudaMemcpyDeviceToHost, s->stream), "children");
   SCK(cudaMemcpyAsync(&next, s->tab.node_next + slot, 4, cudaMemcpyDeviceToHost, s->stream), "children");
   SCK(cudaStreamSynchronize(s->stream), "children");
   if (nodes_used) *nodes_used = (uint32_t)(next - r);
+  const int32_t k = ((ri.y >> 16) & kExpanded) ? (int32_t)(ri.y & 0xffffu) : 0;
+  const int32_t first = (int32_t)ri.x;
   *nchildren = (uint32_t)k;
   if (k <= 0) return GPUAI_OK;
-  std::vector<uint32_t> v(k), sc(k), mv(k), rm(k);
-  SCK(cudaMemcpyAsync(v.data(), s->pool.visits + first, 4 * k, cudaMemcpyDeviceToHost, s->stream), "children");
-  SCK(cudaMemcpyAsync(sc.data(), s->pool.score2 + first, 4 * k, cudaMemcpyDeviceToHost, s->stream), "children");
-  SCK(cudaMemcpyAsync(mv.data(), s->pool.move + first, 4 * k, cudaMemcpyDeviceToHost, s->stream), "children");
-  SCK(cudaMemcpyAsync(rm.data(), s->pool.removed + first, 4 * k, cudaMemcpyDeviceToHost, s->stream), "children");
+  std::vector<uint4> ci(k);
+  SCK(cudaMemcpyAsync(ci.data(), s->pool.info + first, 16 * k, cudaMemcpyDeviceToHost, s->stream), "children");
   SCK(cudaStreamSynchronize(s->stream), "children");
+  std::vector<uint32_t> v(k), sc(k);
+  for (int32_t i = 0; i < k; i++) {
+    v[i] = ci[i].z;
+    sc[i] = ci[i].w;
+  }
   // full move records from the root's move list (same order as the children)
-  const Board b{rb.x, rb.y, rb.z, rb.w};
-  Side sd;
-  make_side(b, sd);
+  gpuai::State root_state;
+  root_state.b = gpuai_board{rb.x, rb.y, rb.z, rb.w};
+  const std::vector<gpuai::Move> all_moves = root_state.getMoves();
   std::vector<gpuai_move> all;
-  for_each_move(sd, jumpers(sd), [&](int from, int to, uint32_t, int jumps, uint32_t dirs) {
-    uint32_t w[8];
-    pack_move(b, from, to, jumps, dirs, w);
-    gpuai_move m;
-    std::memcpy(&m, w, sizeof m);
-    all.push_back(m);
-    return false;
-  });
+  for (const gpuai::Move &m : all_moves) all.push_back(m.m);
   for (uint32_t i = 0; i < (uint32_t)k && i < max_children; i++) {
     if (visits) visits[i] = v[i];
     if (score2) score2[i] = sc[i];
