@@ -381,7 +381,7 @@ def main():
     ap.add_argument("--blocks-per-sm", type=int, default=0, help="resident blocks per SM (0: as many as fit)")
     ap.add_argument("--workload", choices=["playouts", "searches"], default="playouts")
     ap.add_argument("--games", type=int, default=2048, help="searches workload: number of games")
-    ap.add_argument("--leaves", type=int, default=64, help="searches workload: leaves per search per step")
+    ap.add_argument("--leaves", type=int, default=128, help="searches workload: leaves per search per step")
     ap.add_argument("--playouts-per-leaf", type=int, default=8, help="searches workload: playouts per leaf")
     args = ap.parse_args()
     if args.warmup < 3:
