@@ -370,6 +370,26 @@ def run_searches(args):
     print(json.dumps(line), flush=True)
 
 
+def run_serve(args):
+    """Serving loop: Poisson arrivals of search requests on 10K seeded games
+    (0-60 random plies), time budgets U(10, 200) ms, continuous batching;
+    random and reference-heuristic playouts side by side."""
+    from gpu_ai_gb300.serve import simulate
+    from gpu_ai_gb300 import POLICY_RANDOM, POLICY_REF_HEURISTIC
+    res = {}
+    for name, pol in (("random", POLICY_RANDOM), ("ref_heuristic", POLICY_REF_HEURISTIC)):
+        res[name] = simulate(rate=args.rate, n_requests=args.requests, n_games=10000, budget_ms=(10.0, 200.0),
+                             policy=pol, leaves_per_search=args.leaves if args.leaves <= 256 else 64,
+                             playouts_per_leaf=args.playouts_per_leaf)
+    line = {"metric": "serving: search requests with continuous batching", "unit": "ms",
+            "value": res["random"]["latency_ms_p99"], "higher_is_better": False, "n_gpus": 1,
+            "data": "synthetic (seeded games, Poisson arrivals)",
+            "config": {"workload": f"{args.requests} requests at {args.rate} req/s, budgets U(10,200) ms",
+                       "leaves_per_search_per_step": args.leaves, "playouts_per_leaf": args.playouts_per_leaf},
+            "random": res["random"], "ref_heuristic": res["ref_heuristic"]}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -379,7 +399,9 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--block", type=int, default=0, help="threads per block of the playout kernel (0: default)")
     ap.add_argument("--blocks-per-sm", type=int, default=0, help="resident blocks per SM (0: as many as fit)")
-    ap.add_argument("--workload", choices=["playouts", "searches"], default="playouts")
+    ap.add_argument("--workload", choices=["playouts", "searches", "serve"], default="playouts")
+    ap.add_argument("--rate", type=float, default=1000.0, help="serve workload: requests per second")
+    ap.add_argument("--requests", type=int, default=2000, help="serve workload: number of requests")
     ap.add_argument("--games", type=int, default=2048, help="searches workload: number of games")
     ap.add_argument("--leaves", type=int, default=128, help="searches workload: leaves per search per step")
     ap.add_argument("--playouts-per-leaf", type=int, default=8, help="searches workload: playouts per leaf")
@@ -390,6 +412,8 @@ def main():
         run_reference(args)
     elif args.workload == "searches":
         run_searches(args)
+    elif args.workload == "serve":
+        run_serve(args)
     else:
         run_ours(args)
 
