@@ -264,6 +264,9 @@ class Searches:
         return {"moves": moves[:k], "visits": visits[:k], "score2": score2[:k], "nodes": used.value}
 
     def best(self, slot: int):
+        """Most visited root move (None for a finished game) and the child statistics."""
         c = self.children(slot)
+        if len(c["visits"]) == 0:
+            return None, c
         i = int(np.argmax(c["visits"]))
         return c["moves"][i], c

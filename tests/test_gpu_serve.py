@@ -14,8 +14,15 @@ def _req(rid, board, playouts, cap=40000):
     return Request(rid=rid, board=board, arrival=0.0, budget_playouts=playouts, node_capacity=cap)
 
 
+def _live(boards):
+    """Boards whose game is not over."""
+    _, counts = L.genmoves(boards)
+    return boards[(counts > 0) & (((boards[:, 3] >> 8) & 0xff) < 50)]
+
+
 def test_request_same_alone_and_in_mix(lib_built):
-    boards = L.random_positions(17, 40, 0, 60)
+    boards = _live(L.random_positions(17, 60, 0, 60))[:40]
+    assert len(boards) == 40
     srv = SearchServer(max_searches=64, pool_nodes=4_000_000, leaves_per_search=32, playouts_per_leaf=4)
     srv.submit(_req(7, boards[7], 24000))
     srv.drain()
@@ -43,7 +50,7 @@ def test_request_same_alone_and_in_mix(lib_built):
 
 
 def test_admission_waits_for_free_nodes(lib_built):
-    boards = L.random_positions(3, 6, 0, 30)
+    boards = _live(L.random_positions(3, 12, 0, 30))[:6]
     srv = SearchServer(max_searches=16, pool_nodes=25000, leaves_per_search=16, playouts_per_leaf=2)
     for i in range(6):
         srv.submit(_req(i, boards[i], 2000, cap=10000))
