@@ -15,6 +15,7 @@ from .engine import (  # noqa: F401
     POLICY_REF_HEURISTIC,
     START_BOARD,
     Engine,
+    Net,
     Searches,
     GpuAIError,
     header_symbols,
@@ -23,6 +24,7 @@ from .engine import (  # noqa: F401
 
 __all__ = [
     "Engine",
+    "Net",
     "Searches",
     "GpuAIError",
     "load_library",

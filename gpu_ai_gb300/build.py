@@ -29,7 +29,7 @@ NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompil
               "-I" + INCLUDE, "-I" + CSRC] + ARCH
 CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-Wall", "-Wextra", "-pthread", "-I" + INCLUDE, "-I" + CSRC]
 
-CUDA_UNITS = ["kernels.cu", "capi.cu", "noalloc.cu", "search.cu"]
+CUDA_UNITS = ["kernels.cu", "capi.cu", "noalloc.cu", "search.cu", "net.cu"]
 
 
 def nvcc() -> str:

@@ -1,0 +1,1129 @@
+// net.cu -- the policy/value MLP on the sm_103a tensor cores, its training
+// kernels, training labels from GPU playouts, and their C ABI (gpuai_net_*,
+// gpuai_label_positions).  The reference has no learned evaluation; this is
+// the project's own component (its heuristic, src/heuristic.cu:20-49, is the
+// only evaluation function there).
+//
+// Every matrix product is one kernel, gemm_kernel: C = A * B^T with A (M x K)
+// and B (N x K) BF16 and K-major in global memory.  A CTA of four warps
+// computes one 128 x BN tile (BN <= 256): warp 0 streams 64-wide K blocks of A
+// and B through a shared-memory ring with TMA (128-byte swizzle), warp 1 issues
+// tcgen05.mma (M = 128, N = BN, K = 16 per instruction, FP32 accumulators in
+// 256 TMEM columns), then all four warps read the accumulators back (warp w
+// owns TMEM lanes 32w..32w+31, i.e. tile rows) and apply a fused epilogue.
+//
+// Training step on a batch of B rows (a multiple of 128; rows past n are zero):
+//   features      X (B x 192), X^T
+//   F1  X  W1^T  -> H1 = bf16(relu(. + b1)), H1^T
+//   F2  H1 W2^T  -> H2 = bf16(relu(. + b2)), H2^T, vraw = H2 . wv + bv
+//   F3  H2 W3^T  -> logits = . + b3 (FP32)
+//   loss          dZ3 = (softmax - target) / n on the legal (from, to), dZ3^T, dv
+//   B1  dZ3 W3   -> dZ2 = bf16((. + dv wv^T) * [H2 > 0]), dZ2^T
+//   B3  dZ2 W2   -> dZ1^T = bf16(. * [H1 > 0])
+//   B2  dZ3^T H2 -> dW3 partial sums (K = the batch, split over CTAs)
+//   B4  dZ2^T H1 -> dW2 partial sums
+//   B5  dZ1^T X  -> dW1 partial sums
+//   row sums      db1, db2, db3, dwv = H2^T dv, dbv
+//   adam          sums the partials in a fixed order, updates the FP32 master
+//                 parameters, writes the BF16 copies W1..W3 and W2^T, W3^T
+// Every reduction has a fixed order, so a training run is reproducible.
+#include "net.h"
+
+#include "launch.h"
+#include "rules.cuh"
+#include "tc.cuh"
+
+#include <cudaTypedefs.h>
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+
+using bf16 = __nv_bfloat16;
+
+struct gpuai_net {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  uint32_t rows = 0;  // training batch capacity (multiple of 128)
+  std::vector<void *> allocs;
+  float *params = nullptr, *adam_m = nullptr, *adam_v = nullptr, *grad = nullptr;
+  bf16 *W1b = nullptr, *W2b = nullptr, *W3b = nullptr, *W2T = nullptr, *W3T = nullptr;
+  CUtensorMap mW1, mW2, mW3, mW2T, mW3T;
+  uint64_t step = 0;
+  ga::net::Fwd fw;
+  bf16 *Xt = nullptr, *H1t = nullptr, *H2t = nullptr, *dZ3 = nullptr, *dZ3t = nullptr, *dZ2 = nullptr,
+       *dZ2t = nullptr, *dZ1t = nullptr;
+  float *dv = nullptr, *rowloss = nullptr, *loss2 = nullptr, *p1 = nullptr, *p2 = nullptr, *p3 = nullptr;
+  float *gout = nullptr, *value = nullptr;
+  CUtensorMap mXt, mH1t, mH2t, mdZ3, mdZ3t, mdZ2, mdZ2t, mdZ1t;
+  uint32_t *status = nullptr;
+  gpuai_board *in_boards = nullptr;  // staging for host-buffer calls
+  float *in_z = nullptr, *in_q = nullptr;
+  std::mutex mu;
+};
+
+namespace ga {
+namespace net {
+namespace {
+
+enum : uint32_t {
+  kEpiBias = 1u,      // + bias[col]
+  kEpiRelu = 2u,      // max(., 0)
+  kEpiF32 = 4u,       // FP32 row-major store
+  kEpiB16 = 8u,       // BF16 row-major store
+  kEpiB16T = 16u,     // BF16 transposed store: out_t[col * ld_t + row]
+  kEpiMask = 32u,     // * [mask[row][col] > 0] (mask: BF16 ReLU output)
+  kEpiRank1 = 64u,    // + r1_row[row] * r1_col[col]
+  kEpiVdot = 128u,    // vdot_out[row] = sum_col bf16(.) * vdot_w[col] + vdot_b (needs the whole row in one tile)
+  kEpiPartial = 256u  // FP32 row-major store into split-K partial blockIdx.z
+};
+
+struct Epi {
+  uint32_t flags = 0;
+  const float *bias = nullptr;
+  float *out_f32 = nullptr;
+  uint32_t ld_f32 = 0;
+  uint64_t partial_stride = 0;
+  bf16 *out_b = nullptr;
+  uint32_t ld_b = 0;
+  bf16 *out_t = nullptr;
+  uint32_t ld_t = 0;
+  const bf16 *mask = nullptr;
+  uint32_t ld_mask = 0;
+  const float *r1_row = nullptr, *r1_col = nullptr;
+  const float *vdot_w = nullptr, *vdot_b = nullptr;
+  float *vdot_out = nullptr;
+};
+
+struct GemmArgs {
+  uint32_t m_rows;        // rows of A (multiple of 128)
+  uint32_t bn;            // tile width = MMA N (multiple of 16, <= 256)
+  uint32_t kb_per_split;  // 64-wide K blocks per CTA
+  uint32_t stages;        // shared-memory ring depth
+  const uint32_t *dev_rows;  // optional device row count: tiles past it do nothing
+  uint32_t *status;
+  Epi e;
+};
+
+constexpr uint32_t kBM = 128, kBK = 64, kTmemCols = 256, kMaxStages = 4;
+constexpr uint32_t kABytes = kBM * kBK * 2;  // one A stage: 16 KiB
+constexpr uint32_t kSmemLimit = 227u * 1024u;
+
+__device__ __forceinline__ uint32_t pack2(float a, float b) {
+  __nv_bfloat162 h = __floats2bfloat162_rn(a, b);  // a in the low half
+  return *reinterpret_cast<uint32_t *>(&h);
+}
+
+__device__ __forceinline__ float lo_bf(uint32_t w) { return __uint_as_float(w << 16); }
+__device__ __forceinline__ float hi_bf(uint32_t w) { return __uint_as_float(w & 0xffff0000u); }
+__device__ __forceinline__ bool positive_bf(uint32_t h16) { return (h16 & 0x8000u) == 0 && (h16 & 0x7fffu) != 0; }
+
+// Epilogue of 32 consecutive columns col0.. of one row.
+__device__ __forceinline__ void epilogue32(const Epi &e, float (&v)[32], uint32_t row, uint32_t col0,
+                                           uint32_t split, float &vsum) {
+  const uint32_t f = e.flags;
+  if (f & kEpiBias) {
+#pragma unroll
+    for (int j = 0; j < 32; j++) v[j] += __ldg(&e.bias[col0 + j]);
+  }
+  if (f & kEpiRank1) {
+    const float r = e.r1_row[row];
+#pragma unroll
+    for (int j = 0; j < 32; j++) v[j] = fmaf(r, __ldg(&e.r1_col[col0 + j]), v[j]);
+  }
+  if (f & kEpiRelu) {
+#pragma unroll
+    for (int j = 0; j < 32; j++) v[j] = fmaxf(v[j], 0.0f);
+  }
+  if (f & kEpiMask) {
+    const uint4 *mp = reinterpret_cast<const uint4 *>(e.mask + (size_t)row * e.ld_mask + col0);
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      const uint4 m = mp[q];
+      const uint32_t w[4] = {m.x, m.y, m.z, m.w};
+#pragma unroll
+      for (int t = 0; t < 4; t++) {
+        if (!positive_bf(w[t] & 0xffffu)) v[8 * q + 2 * t] = 0.0f;
+        if (!positive_bf(w[t] >> 16)) v[8 * q + 2 * t + 1] = 0.0f;
+      }
+    }
+  }
+  if (f & (kEpiF32 | kEpiPartial)) {
+    float *o = e.out_f32 + ((f & kEpiPartial) ? (uint64_t)split * e.partial_stride : 0ull) +
+               (size_t)row * e.ld_f32 + col0;
+#pragma unroll
+    for (int q = 0; q < 8; q++)
+      reinterpret_cast<float4 *>(o)[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+  }
+  if (f & (kEpiB16 | kEpiB16T | kEpiVdot)) {
+    uint32_t p[16];
+#pragma unroll
+    for (int t = 0; t < 16; t++) p[t] = pack2(v[2 * t], v[2 * t + 1]);
+    if (f & kEpiB16) {
+      uint4 *o = reinterpret_cast<uint4 *>(e.out_b + (size_t)row * e.ld_b + col0);
+#pragma unroll
+      for (int q = 0; q < 4; q++) o[q] = make_uint4(p[4 * q], p[4 * q + 1], p[4 * q + 2], p[4 * q + 3]);
+    }
+    if (f & kEpiB16T) {
+      uint16_t *o = reinterpret_cast<uint16_t *>(e.out_t) + (size_t)col0 * e.ld_t + row;
+#pragma unroll
+      for (int t = 0; t < 16; t++) {
+        o[(size_t)(2 * t) * e.ld_t] = (uint16_t)(p[t] & 0xffffu);
+        o[(size_t)(2 * t + 1) * e.ld_t] = (uint16_t)(p[t] >> 16);
+      }
+    }
+    if (f & kEpiVdot) {
+#pragma unroll
+      for (int t = 0; t < 16; t++) {
+        vsum = fmaf(lo_bf(p[t]), __ldg(&e.vdot_w[col0 + 2 * t]), vsum);
+        vsum = fmaf(hi_bf(p[t]), __ldg(&e.vdot_w[col0 + 2 * t + 1]), vsum);
+      }
+    }
+  }
+}
+
+__global__ void __launch_bounds__(128, 1)
+    gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, const GemmArgs g) {
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023u) & ~(uintptr_t)1023u);
+  const uint32_t bn = g.bn, stage_bytes = kABytes + bn * 128u, nst = g.stages;
+  uint64_t *full = reinterpret_cast<uint64_t *>(smem + nst * stage_bytes);
+  uint64_t *empty = full + nst;
+  uint64_t *accf = empty + nst;
+  uint32_t *tslot = reinterpret_cast<uint32_t *>(accf + 1);
+  uint32_t *s_err = tslot + 1;
+  const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+  const uint32_t row0 = blockIdx.x * kBM;
+  uint32_t rows = g.m_rows;
+  if (g.dev_rows) {
+    const uint32_t d = *g.dev_rows;
+    rows = d < rows ? d : rows;
+    if (row0 >= rows) return;  // uniform over the CTA, before any barrier or TMEM use
+  }
+  if (threadIdx.x == 0) {
+    for (uint32_t s = 0; s < nst; s++) {
+      tc::mbar_init(&full[s], 1);
+      tc::mbar_init(&empty[s], 1);
+    }
+    tc::mbar_init(accf, 1);
+    *s_err = 0;
+    tc::fence_mbar_init();
+    tc::tma_prefetch_map(&tmA);
+    tc::tma_prefetch_map(&tmB);
+  }
+  if (warp == 2) tc::tmem_alloc(tslot, kTmemCols);
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = *tslot;
+  const uint32_t nkb = g.kb_per_split, kb0 = blockIdx.z * nkb;
+  uint32_t issued = 0;
+
+  if (warp == 0) {
+    if (lane == 0) {  // TMA producer
+      for (uint32_t i = 0; i < nkb; i++) {
+        const uint32_t s = i % nst;
+        if (i >= nst && !tc::mbar_wait(&empty[s], ((i / nst) - 1u) & 1u)) {
+          atomicOr(s_err, 1u);
+          break;
+        }
+        uint8_t *sa = smem + s * stage_bytes;
+        tc::mbar_arrive_expect_tx(&full[s], stage_bytes);
+        tc::tma_load_2d(sa, &tmA, &full[s], (int32_t)((kb0 + i) * kBK), (int32_t)row0);
+        tc::tma_load_2d(sa + kABytes, &tmB, &full[s], (int32_t)((kb0 + i) * kBK), (int32_t)(blockIdx.y * bn));
+        issued = i + 1;
+      }
+    }
+    __syncwarp();
+  } else if (warp == 1) {
+    if (lane == 0) {  // MMA issuer
+      const uint32_t idesc = tc::idesc_bf16_f32(kBM, bn);
+      for (uint32_t i = 0; i < nkb; i++) {
+        const uint32_t s = i % nst;
+        if (!tc::mbar_wait(&full[s], (i / nst) & 1u)) {
+          atomicOr(s_err, 1u);
+          break;
+        }
+        tc::fence_after_sync();
+        const uint32_t sa = tc::smem_u32(smem + s * stage_bytes), sb = sa + kABytes;
+#pragma unroll
+        for (uint32_t kk = 0; kk < kBK / 16; kk++)
+          tc::mma_bf16(tmem, tc::sdesc_sw128(sa + kk * 32u), tc::sdesc_sw128(sb + kk * 32u), idesc,
+                       (i | kk) != 0u ? 1u : 0u);
+        tc::mma_commit(&empty[s]);  // the stage is free once these MMAs have read it
+      }
+      tc::mma_commit(accf);
+    }
+    __syncwarp();
+  }
+
+  // epilogue: thread = tile row warp*32 + lane
+  if (!tc::mbar_wait(accf, 0)) atomicOr(s_err, 1u);
+  __syncwarp();  // lanes leave the wait one by one; tcgen05.ld needs the whole warp
+  tc::fence_after_sync();
+  const uint32_t row = row0 + warp * 32u + lane;
+  const bool row_ok = row < rows && *s_err == 0;
+  float vsum = 0.0f;
+  for (uint32_t c = 0; c < bn; c += 32) {
+    float v[32];
+    tc::tmem_load32(tmem + ((warp * 32u) << 16) + c, v);  // warp-collective: every lane takes part
+    if (row_ok) epilogue32(g.e, v, row, blockIdx.y * bn + c, blockIdx.z, vsum);
+  }
+  if (row_ok && (g.e.flags & kEpiVdot)) g.e.vdot_out[row] = vsum + g.e.vdot_b[0];
+
+  tc::fence_before_sync();
+  __syncthreads();
+  if (*s_err) {
+    if (threadIdx.x == 0) {
+      atomicOr(g.status, kStatusNetWait);
+      // let loads still in flight land before the CTA's shared memory goes away
+      for (uint32_t i = issued > nst ? issued - nst : 0u; i < issued; i++) tc::mbar_wait(&full[i % nst], (i / nst) & 1u);
+    }
+    __syncthreads();
+  }
+  if (warp == 2) {
+    tc::fence_after_sync();
+    tc::tmem_dealloc(tmem, kTmemCols);
+  }
+}
+
+// ---- small kernels
+
+__device__ __forceinline__ uint32_t one_pair(uint32_t bits, int t) {
+  return (((bits >> (2 * t)) & 1u) ? 0x3F80u : 0u) | (((bits >> (2 * t + 1)) & 1u) ? 0x3F800000u : 0u);
+}
+
+// X[r] = the 192 features of board r (zero rows past n); X^T optional.
+__global__ void features_kernel(const gpuai_board *boards, uint32_t n, const uint32_t *dev_n, uint32_t rows, bf16 *X,
+                                bf16 *Xt, uint32_t ldt) {
+  const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= rows) return;
+  uint32_t nn = n;
+  if (dev_n) nn = *dev_n < rows ? *dev_n : rows;
+  uint32_t pl[4] = {0u, 0u, 0u, 0u}, side = 0;
+  if (r < nn) {
+    const uint4 b = __ldg(reinterpret_cast<const uint4 *>(boards) + r);
+    side = b.w & 1u;
+    const uint32_t own = side ? b.y : b.x, opp = side ? b.x : b.y;
+    pl[0] = own & ~b.z;
+    pl[1] = own & b.z;
+    pl[2] = opp & ~b.z;
+    pl[3] = opp & b.z;
+  }
+  uint4 *dst = reinterpret_cast<uint4 *>(X + (size_t)r * kInPad);
+#pragma unroll
+  for (uint32_t c = 0; c < kInPad / 8; c++) {
+    uint32_t bits = 0;
+    if (c < 16) bits = (pl[c >> 2] >> ((c & 3u) * 8u)) & 0xffu;
+    else if (c == 16) bits = side;
+    dst[c] = make_uint4(one_pair(bits, 0), one_pair(bits, 1), one_pair(bits, 2), one_pair(bits, 3));
+  }
+  if (Xt) {
+    uint16_t *xt = reinterpret_cast<uint16_t *>(Xt);
+    for (uint32_t f = 0; f < kInPad; f++) {
+      const uint32_t bit = f < 128 ? (pl[f >> 5] >> (f & 31u)) & 1u : (f == 128 ? side : 0u);
+      xt[(size_t)f * ldt + r] = bit ? 0x3F80u : 0u;
+    }
+  }
+}
+
+// One thread per row: value and policy loss terms and their gradients.
+__global__ void loss_kernel(const gpuai_board *boards, const float *z, const float *q, uint32_t n, uint32_t rows,
+                            float tau, float vcoef, const float *logits, const float *vraw, bf16 *dZ3, bf16 *dZ3t,
+                            uint32_t ldt, float *dv, float *rowloss) {
+  const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= rows) return;
+  if (r >= n) {
+    dv[r] = 0.0f;
+    rowloss[2 * r] = rowloss[2 * r + 1] = 0.0f;
+    return;
+  }
+  const float inv_n = 1.0f / (float)n;
+  const float th = tanhf(vraw[r]);
+  const float e = th - z[r];
+  dv[r] = vcoef * 2.0f * e * (1.0f - th * th) * inv_n;
+  rowloss[2 * r + 1] = e * e;
+  float ce = 0.0f;
+  const uint4 bv = __ldg(reinterpret_cast<const uint4 *>(boards) + r);
+  const Board b{bv.x, bv.y, bv.z, bv.w};
+  Side sd;
+  make_side(b, sd);
+  const uint32_t J = jumpers(sd);
+  const int k = count_moves(sd, J);
+  if (k >= 1 && k <= (int)kMaxMoves) {
+    uint16_t pair[kMaxMoves] = {};
+    int np = 0;
+    float tp[kMaxMoves];
+    const float *qr = q + (size_t)r * kMaxMoves;
+    float qmax = -3.0e38f;
+    for (int m = 0; m < k; m++) qmax = fmaxf(qmax, qr[m]);
+    float tsum = 0.0f;
+    for (int m = 0; m < k; m++) tsum += expf((qr[m] - qmax) / tau);
+    int m = 0;
+    for_each_move(sd, J, [&](int from, int to, uint32_t, int, uint32_t) {
+      const uint16_t pi = (uint16_t)(from * 32 + to);
+      const float t = expf((qr[m] - qmax) / tau) / tsum;
+      int u = 0;
+      while (u < np && pair[u] != pi) u++;
+      if (u == np) {
+        pair[np] = pi;
+        tp[np] = 0.0f;
+        np++;
+      }
+      tp[u] += t;
+      m++;
+      return false;
+    });
+    const float *lr = logits + (size_t)r * kOut;
+    float lmax = -3.0e38f;
+    for (int u = 0; u < np; u++) lmax = fmaxf(lmax, lr[pair[u]]);
+    float s = 0.0f;
+    for (int u = 0; u < np; u++) s += expf(lr[pair[u]] - lmax);
+    const float logz = lmax + logf(s);
+    for (int u = 0; u < np; u++) {
+      const float lp = lr[pair[u]] - logz;
+      ce -= tp[u] * lp;
+      const bf16 gq = __float2bfloat16_rn((expf(lp) - tp[u]) * inv_n);
+      dZ3[(size_t)r * kOut + pair[u]] = gq;
+      dZ3t[(size_t)pair[u] * ldt + r] = gq;
+    }
+  }
+  rowloss[2 * r] = ce;
+}
+
+// out[row] = sum over the first ncols columns of M[row] (times vec[col] if
+// given); one warp per row, fixed order.
+__global__ void rowsum_kernel(const bf16 *M, uint32_t nrows, uint32_t ncols, uint32_t ld, const float *vec,
+                              float *out) {
+  const uint32_t row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31u;
+  if (row >= nrows) return;
+  const bf16 *p = M + (size_t)row * ld;
+  float s = 0.0f;
+  for (uint32_t c = lane * 8u; c < ncols; c += 256u) {
+    const uint4 u = *reinterpret_cast<const uint4 *>(p + c);
+    const uint32_t w[4] = {u.x, u.y, u.z, u.w};
+#pragma unroll
+    for (int t = 0; t < 4; t++) {
+      const float a = lo_bf(w[t]), b = hi_bf(w[t]);
+      s += vec ? a * vec[c + 2 * t] : a;
+      s += vec ? b * vec[c + 2 * t + 1] : b;
+    }
+  }
+  for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if (lane == 0) out[row] = s;
+}
+
+// out[0] = sum of v[0..n) (one warp, fixed order).
+__global__ void vecsum_kernel(const float *v, uint32_t n, float *out) {
+  const uint32_t lane = threadIdx.x & 31u;
+  float s = 0.0f;
+  for (uint32_t i = lane; i < n; i += 32) s += v[i];
+  for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if (lane == 0) out[0] = s;
+}
+
+// loss2 = {mean policy cross entropy, mean squared value error} (one block of 256).
+__global__ void loss_reduce_kernel(const float *rowloss, uint32_t n, float *loss2) {
+  __shared__ float sp[256], sv[256];
+  float a = 0.0f, b = 0.0f;
+  for (uint32_t i = threadIdx.x; i < n; i += 256) {
+    a += rowloss[2 * i];
+    b += rowloss[2 * i + 1];
+  }
+  sp[threadIdx.x] = a;
+  sv[threadIdx.x] = b;
+  __syncthreads();
+  for (uint32_t o = 128; o; o >>= 1) {
+    if (threadIdx.x < o) {
+      sp[threadIdx.x] += sp[threadIdx.x + o];
+      sv[threadIdx.x] += sv[threadIdx.x + o];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    loss2[0] = n ? sp[0] / (float)n : 0.0f;
+    loss2[1] = n ? sv[0] / (float)n : 0.0f;
+  }
+}
+
+struct AdamArgs {
+  float *w, *m, *v;
+  const float *g_direct;  // bias / value-head gradients (parameter layout)
+  const float *p1, *p2, *p3;
+  uint32_t s1, s2, s3;    // split-K partial counts of dW1, dW2, dW3
+  float lr, bc1, bc2;
+  uint32_t mode;          // 0 update, 1 write the gradient to g_out, 2 refresh the BF16 copies only
+  float *g_out;
+  bf16 *W1b, *W2b, *W3b, *W2T, *W3T;
+};
+
+constexpr float kBeta1 = 0.9f, kBeta2 = 0.999f, kAdamEps = 1e-8f;
+
+__global__ void adam_kernel(AdamArgs a) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= kParams) return;
+  float w = a.w[i];
+  if (a.mode != 2) {
+    float g = 0.0f;
+    if (i < oB1) {
+      for (uint32_t s = 0; s < a.s1; s++) g += a.p1[(size_t)s * (kH * kInPad) + (i - oW1)];
+    } else if (i >= oW2 && i < oB2) {
+      for (uint32_t s = 0; s < a.s2; s++) g += a.p2[(size_t)s * (kH * kH) + (i - oW2)];
+    } else if (i >= oW3 && i < oB3) {
+      for (uint32_t s = 0; s < a.s3; s++) g += a.p3[(size_t)s * (kOut * kH) + (i - oW3)];
+    } else {
+      g = a.g_direct[i];
+    }
+    if (a.mode == 1) {
+      a.g_out[i] = g;
+      return;
+    }
+    const float m = kBeta1 * a.m[i] + (1.0f - kBeta1) * g;
+    const float v = kBeta2 * a.v[i] + (1.0f - kBeta2) * g * g;
+    a.m[i] = m;
+    a.v[i] = v;
+    w -= a.lr * (m / a.bc1) / (sqrtf(v / a.bc2) + kAdamEps);
+    a.w[i] = w;
+  }
+  const bf16 wb = __float2bfloat16_rn(w);
+  if (i < oB1) {
+    a.W1b[i - oW1] = wb;
+  } else if (i >= oW2 && i < oB2) {
+    const size_t j = i - oW2, r = j / kH, c = j % kH;
+    a.W2b[j] = wb;
+    a.W2T[c * kH + r] = wb;
+  } else if (i >= oW3 && i < oB3) {
+    const size_t j = i - oW3, r = j / kH, c = j % kH;
+    a.W3b[j] = wb;
+    a.W3T[c * kOut + r] = wb;
+  }
+}
+
+__global__ void tanh_kernel(const float *x, uint32_t n, float *y) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) y[i] = tanhf(x[i]);
+}
+
+// ---- training labels
+
+constexpr uint32_t kLabelSlots = kMaxMoves;  // child slots per position
+
+// Child boards and playout offsets: position i owns playouts
+// [i*P, (i+1)*P); move m of its k moves gets P/k (+1 for m < P%k) of them.  A
+// position that is over (or has more than 32 moves) gives all P playouts to
+// slot 0, a copy of itself, and is marked with nmoves 0.
+__global__ void label_children_kernel(const gpuai_board *pos, uint32_t n, uint32_t P, Board *children,
+                                      uint32_t *offsets, uint8_t *nmoves) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const uint4 bv = __ldg(reinterpret_cast<const uint4 *>(pos) + i);
+  const Board b{bv.x, bv.y, bv.z, bv.w};
+  Side sd;
+  make_side(b, sd);
+  const uint32_t J = jumpers(sd);
+  int k = ((b.meta >> 8) & 0xffu) >= (uint32_t)kDrawPlies ? 0 : count_moves(sd, J);
+  if (k < 0 || k > (int)kLabelSlots) k = 0;
+  Board *ch = children + (size_t)i * kLabelSlots;
+  uint32_t *off = offsets + (size_t)i * kLabelSlots;
+  const uint32_t base = i * P;
+  int m = 0;
+  if (k > 0) {
+    for_each_move(sd, J, [&](int from, int to, uint32_t removed, int, uint32_t) {
+      Board c = b;
+      apply_move(c, from, to, removed);
+      ch[m++] = c;
+      return false;
+    });
+  }
+  for (; m < (int)kLabelSlots; m++) ch[m] = b;
+  const uint32_t uk = (uint32_t)k;
+  for (uint32_t s = 0; s < kLabelSlots; s++) {
+    uint32_t o;
+    if (uk == 0) o = s == 0 ? base : base + P;
+    else o = s >= uk ? base + P : base + s * (P / uk) + (s < P % uk ? s : P % uk);
+    off[s] = o;
+  }
+  nmoves[i] = (uint8_t)uk;
+  if (i == n - 1) offsets[(size_t)n * kLabelSlots] = n * P;
+}
+
+// One warp per position: move values and the position value for its side to move.
+__global__ void label_reduce_kernel(const gpuai_board *pos, const int8_t *out, const uint32_t *offsets,
+                                    const uint8_t *nmoves, uint32_t n, uint32_t P, float *value, float *q) {
+  const uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31u;
+  if (i >= n) return;
+  const uint32_t k = nmoves[i];
+  const float sign = (pos[i].meta & 1u) ? -1.0f : 1.0f;  // outcome +1 = PLAYER_1 won
+  int total = 0;
+  for (uint32_t m = 0; m < kLabelSlots; m++) {
+    float qm = 0.0f;
+    if (m < k) {
+      const uint32_t a = offsets[(size_t)i * kLabelSlots + m], e = offsets[(size_t)i * kLabelSlots + m + 1];
+      int s = 0;
+      for (uint32_t j = a + lane; j < e; j += 32) s += out[j];
+      for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+      total += s;
+      qm = sign * (float)s / (float)(e - a);
+    }
+    if (lane == 0) q[(size_t)i * kMaxMoves + m] = qm;
+  }
+  if (lane == 0) value[i] = k ? sign * (float)total / (float)P : 0.0f;
+}
+
+// ---- host side
+
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  });
+  return fn;
+}
+
+// Tensor map of a K-major BF16 matrix (rows x k, row pitch k elements) read
+// in boxes of 64 x box_rows with the 128-byte swizzle.
+cudaError_t make_map(CUtensorMap *m, const void *base, uint64_t rows, uint64_t k, uint32_t box_rows) {
+  auto fn = encode_fn();
+  if (!fn) return cudaErrorNotSupported;
+  if (k % kBK || box_rows == 0 || box_rows > 256 || reinterpret_cast<uintptr_t>(base) % 16)
+    return cudaErrorInvalidValue;
+  const cuuint64_t dims[2] = {k, rows};
+  const cuuint64_t strides[1] = {k * 2};
+  const cuuint32_t box[2] = {kBK, box_rows};
+  const cuuint32_t es[2] = {1, 1};
+  const CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void *>(base), dims, strides, box, es,
+                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                        CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+}
+
+cudaError_t gemm(const CUtensorMap &a, const CUtensorMap &b, uint32_t m_rows, uint32_t n_total, uint32_t bn,
+                 uint32_t kb_total, uint32_t splits, const uint32_t *dev_rows, uint32_t *status, const Epi &e,
+                 cudaStream_t s) {
+  if (m_rows % kBM || bn % 16 || bn == 0 || bn > kTmemCols || n_total % bn || splits == 0 || kb_total % splits)
+    return cudaErrorInvalidValue;
+  GemmArgs g;
+  g.m_rows = m_rows;
+  g.bn = bn;
+  g.kb_per_split = kb_total / splits;
+  g.stages = g.kb_per_split < kMaxStages ? g.kb_per_split : kMaxStages;
+  g.dev_rows = dev_rows;
+  g.status = status;
+  g.e = e;
+  const uint32_t smem = g.stages * (kABytes + bn * 128u) + 1024u + 128u;
+  if (smem > kSmemLimit) return cudaErrorInvalidValue;
+  gemm_kernel<<<dim3(m_rows / kBM, n_total / bn, splits), 128, smem, s>>>(a, b, g);
+  return cudaGetLastError();
+}
+
+uint32_t pick_splits(uint32_t kb, uint32_t target) {
+  for (uint32_t s = target; s > 1; s--)
+    if (kb % s == 0 && kb / s >= 2) return s;
+  return 1;
+}
+
+constexpr uint32_t kSplit3 = 16, kSplit2 = 32, kSplit1 = 32;
+
+template <class T>
+cudaError_t dalloc(std::vector<void *> &allocs, T **p, size_t n) {
+  void *q = nullptr;
+  cudaError_t e = cudaMalloc(&q, n * sizeof(T) + 256);
+  if (e == cudaSuccess) {
+    allocs.push_back(q);
+    *p = static_cast<T *>(q);
+  }
+  return e;
+}
+
+uint32_t round128(uint32_t n) { return (n + 127u) / 128u * 128u; }
+
+}  // namespace
+
+cudaError_t fwd_alloc(Fwd &w, uint32_t rows, std::vector<void *> &allocs) {
+  w.rows = round128(rows ? rows : 1);
+  cudaError_t e = dalloc(allocs, &w.X, (size_t)w.rows * kInPad);
+  if (e == cudaSuccess) e = dalloc(allocs, &w.H1, (size_t)w.rows * kH);
+  if (e == cudaSuccess) e = dalloc(allocs, &w.H2, (size_t)w.rows * kH);
+  if (e == cudaSuccess) e = dalloc(allocs, &w.logits, (size_t)w.rows * kOut);
+  if (e == cudaSuccess) e = dalloc(allocs, &w.vraw, (size_t)w.rows);
+  if (e == cudaSuccess) e = make_map(&w.mX, w.X, w.rows, kInPad, kBM);
+  if (e == cudaSuccess) e = make_map(&w.mH1, w.H1, w.rows, kH, kBM);
+  if (e == cudaSuccess) e = make_map(&w.mH2, w.H2, w.rows, kH, kBM);
+  return e;
+}
+
+namespace {
+
+// Forward through the three layers; with `train`, also the transposed
+// activations the backward pass reads.
+cudaError_t forward_impl(const gpuai_net *net, Fwd &w, const gpuai_board *boards, uint32_t n, const uint32_t *dev_n,
+                         uint32_t rows, uint32_t *status, bool train, cudaStream_t s) {
+  const float *P = net->params;
+  features_kernel<<<(rows + 127) / 128, 128, 0, s>>>(boards, n, dev_n, rows, w.X, train ? net->Xt : nullptr,
+                                                     net->rows);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  Epi e1;
+  e1.flags = kEpiBias | kEpiRelu | kEpiB16 | (train ? kEpiB16T : 0u);
+  e1.bias = P + oB1;
+  e1.out_b = w.H1;
+  e1.ld_b = kH;
+  e1.out_t = net->H1t;
+  e1.ld_t = net->rows;
+  if ((e = gemm(w.mX, net->mW1, rows, kH, kH, kInPad / kBK, 1, dev_n, status, e1, s)) != cudaSuccess) return e;
+  Epi e2 = e1;
+  e2.flags |= kEpiVdot;
+  e2.bias = P + oB2;
+  e2.out_b = w.H2;
+  e2.out_t = net->H2t;
+  e2.vdot_w = P + oWV;
+  e2.vdot_b = P + oBV;
+  e2.vdot_out = w.vraw;
+  if ((e = gemm(w.mH1, net->mW2, rows, kH, kH, kH / kBK, 1, dev_n, status, e2, s)) != cudaSuccess) return e;
+  Epi e3;
+  e3.flags = kEpiBias | kEpiF32;
+  e3.bias = P + oB3;
+  e3.out_f32 = w.logits;
+  e3.ld_f32 = kOut;
+  return gemm(w.mH2, net->mW3, rows, kOut, kH, kH / kBK, 1, dev_n, status, e3, s);
+}
+
+// Forward + backward on rows [0, n) of the training workspace; gradients are
+// left in the partial buffers and net->grad.
+cudaError_t backward_impl(gpuai_net *net, const gpuai_board *boards, const float *z, const float *q, uint32_t n,
+                          float tau, float vcoef, uint32_t *splits, cudaStream_t s) {
+  const uint32_t B = round128(n), L = net->rows;
+  const float *P = net->params;
+  cudaError_t e = forward_impl(net, net->fw, boards, n, nullptr, B, net->status, true, s);
+  if (e != cudaSuccess) return e;
+  if ((e = cudaMemsetAsync(net->dZ3, 0, (size_t)B * kOut * sizeof(bf16), s)) != cudaSuccess) return e;
+  if ((e = cudaMemset2DAsync(net->dZ3t, (size_t)L * sizeof(bf16), 0, (size_t)B * sizeof(bf16), kOut, s)) !=
+      cudaSuccess)
+    return e;
+  loss_kernel<<<B / 128, 128, 0, s>>>(boards, z, q, n, B, tau, vcoef, net->fw.logits, net->fw.vraw, net->dZ3,
+                                      net->dZ3t, L, net->dv, net->rowloss);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  Epi b1;
+  b1.flags = kEpiRank1 | kEpiMask | kEpiB16 | kEpiB16T;
+  b1.r1_row = net->dv;
+  b1.r1_col = P + oWV;
+  b1.mask = net->fw.H2;
+  b1.ld_mask = kH;
+  b1.out_b = net->dZ2;
+  b1.ld_b = kH;
+  b1.out_t = net->dZ2t;
+  b1.ld_t = L;
+  if ((e = gemm(net->mdZ3, net->mW3T, B, kH, kH, kOut / kBK, 1, nullptr, net->status, b1, s)) != cudaSuccess)
+    return e;
+  Epi b3;
+  b3.flags = kEpiMask | kEpiB16T;
+  b3.mask = net->fw.H1;
+  b3.ld_mask = kH;
+  b3.out_t = net->dZ1t;
+  b3.ld_t = L;
+  if ((e = gemm(net->mdZ2, net->mW2T, B, kH, kH, kH / kBK, 1, nullptr, net->status, b3, s)) != cudaSuccess)
+    return e;
+  const uint32_t kb = B / kBK;
+  splits[2] = pick_splits(kb, kSplit3);
+  splits[1] = pick_splits(kb, kSplit2);
+  splits[0] = pick_splits(kb, kSplit1);
+  Epi b2;
+  b2.flags = kEpiPartial;
+  b2.out_f32 = net->p3;
+  b2.ld_f32 = kH;
+  b2.partial_stride = (uint64_t)kOut * kH;
+  if ((e = gemm(net->mdZ3t, net->mH2t, kOut, kH, kH, kb, splits[2], nullptr, net->status, b2, s)) != cudaSuccess)
+    return e;
+  Epi b4;
+  b4.flags = kEpiPartial;
+  b4.out_f32 = net->p2;
+  b4.ld_f32 = kH;
+  b4.partial_stride = (uint64_t)kH * kH;
+  if ((e = gemm(net->mdZ2t, net->mH1t, kH, kH, kH, kb, splits[1], nullptr, net->status, b4, s)) != cudaSuccess)
+    return e;
+  Epi b5;
+  b5.flags = kEpiPartial;
+  b5.out_f32 = net->p1;
+  b5.ld_f32 = kInPad;
+  b5.partial_stride = (uint64_t)kH * kInPad;
+  if ((e = gemm(net->mdZ1t, net->mXt, kH, kInPad, kInPad, kb, splits[0], nullptr, net->status, b5, s)) !=
+      cudaSuccess)
+    return e;
+  rowsum_kernel<<<kH / 4, 128, 0, s>>>(net->dZ1t, kH, B, L, nullptr, net->grad + oB1);
+  rowsum_kernel<<<kH / 4, 128, 0, s>>>(net->dZ2t, kH, B, L, nullptr, net->grad + oB2);
+  rowsum_kernel<<<kOut / 4, 128, 0, s>>>(net->dZ3t, kOut, B, L, nullptr, net->grad + oB3);
+  rowsum_kernel<<<kH / 4, 128, 0, s>>>(net->H2t, kH, B, L, net->dv, net->grad + oWV);
+  vecsum_kernel<<<1, 32, 0, s>>>(net->dv, B, net->grad + oBV);
+  loss_reduce_kernel<<<1, 256, 0, s>>>(net->rowloss, n, net->loss2);
+  return cudaGetLastError();
+}
+
+cudaError_t run_adam(gpuai_net *net, uint32_t mode, const uint32_t *splits, float lr, cudaStream_t s) {
+  AdamArgs a;
+  a.w = net->params;
+  a.m = net->adam_m;
+  a.v = net->adam_v;
+  a.g_direct = net->grad;
+  a.p1 = net->p1;
+  a.p2 = net->p2;
+  a.p3 = net->p3;
+  a.s1 = splits ? splits[0] : 0;
+  a.s2 = splits ? splits[1] : 0;
+  a.s3 = splits ? splits[2] : 0;
+  a.lr = lr;
+  a.bc1 = (float)(1.0 - std::pow(0.9, (double)net->step));
+  a.bc2 = (float)(1.0 - std::pow(0.999, (double)net->step));
+  a.mode = mode;
+  a.g_out = net->gout;
+  a.W1b = net->W1b;
+  a.W2b = net->W2b;
+  a.W3b = net->W3b;
+  a.W2T = net->W2T;
+  a.W3T = net->W3T;
+  adam_kernel<<<(uint32_t)((kParams + 255) / 256), 256, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+int err(int code, const std::string &m) { return ga::record_error(code, m.c_str()); }
+int cuda_err(cudaError_t e, const char *what) {
+  return err(e == cudaErrorMemoryAllocation ? GPUAI_ERR_OOM : GPUAI_ERR_CUDA,
+             std::string("net: ") + what + ": " + cudaGetErrorString(e));
+}
+
+#define NCK(call, what)                               \
+  do {                                                \
+    cudaError_t e_ = (call);                          \
+    if (e_ != cudaSuccess) return cuda_err(e_, what); \
+  } while (0)
+
+int check_status(gpuai_net *net) {
+  uint32_t st = 0;
+  NCK(cudaMemcpyAsync(&st, net->status, sizeof st, cudaMemcpyDeviceToHost, net->stream), "status read");
+  NCK(cudaStreamSynchronize(net->stream), "net kernels");
+  if (st) {
+    NCK(cudaMemsetAsync(net->status, 0, sizeof(uint32_t), net->stream), "status clear");
+    return err(GPUAI_ERR_LIMIT, "net: a tensor-core kernel gave up waiting (status " + std::to_string(st) + ")");
+  }
+  return GPUAI_OK;
+}
+
+// Glorot-uniform initial parameters from Philox stream (seed, i, 7).
+void init_params(std::vector<float> &p, uint64_t seed) {
+  p.assign(kParams, 0.0f);
+  auto fill = [&](size_t off, uint32_t rows, uint32_t cols, uint32_t used_cols, uint32_t fan_in, uint32_t fan_out) {
+    const double bound = std::sqrt(6.0 / (double)(fan_in + fan_out));
+    for (uint32_t r = 0; r < rows; r++)
+      for (uint32_t c = 0; c < used_cols; c++) {
+        const size_t i = off + (size_t)r * cols + c;
+        uint32_t ctr[4] = {0u, (uint32_t)i, (uint32_t)(i >> 32), 7u};
+        philox4x32_10(ctr, (uint32_t)seed, (uint32_t)(seed >> 32));
+        const double u = (double)(ctr[0] >> 8) * (1.0 / 16777216.0);
+        p[i] = (float)((2.0 * u - 1.0) * bound);
+      }
+  };
+  fill(oW1, kH, kInPad, kIn, kIn, kH);
+  fill(oW2, kH, kH, kH, kH, kH);
+  fill(oW3, kOut, kH, kH, kH, kOut);
+  fill(oWV, 1, kH, kH, kH, 1);
+}
+
+struct Header {
+  char magic[8];
+  uint32_t version, features, in_pad, hidden, logits, nparams;
+  uint64_t step;
+  uint8_t reserved[24];
+};
+static_assert(sizeof(Header) == 64, "header size");
+
+}  // namespace
+
+int device_of(const gpuai_net *net) { return net->device; }
+
+cudaError_t forward(const gpuai_net *net, Fwd &w, const gpuai_board *boards, uint32_t n, const uint32_t *dev_n,
+                    uint32_t *status, cudaStream_t s) {
+  return forward_impl(net, w, boards, n, dev_n, dev_n ? w.rows : round128(n), status, false, s);
+}
+
+}  // namespace net
+}  // namespace ga
+
+using namespace ga::net;
+
+extern "C" {
+
+int gpuai_net_create(int device, uint32_t max_batch, uint64_t init_seed, gpuai_net **out) {
+  if (!out) return err(GPUAI_ERR_INVALID, "gpuai_net_create: out is NULL");
+  *out = nullptr;
+  if (max_batch == 0 || max_batch > (1u << 20))
+    return err(GPUAI_ERR_INVALID, "gpuai_net_create: max_batch must be in 1..2^20");
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || device < 0 || device >= count)
+    return err(GPUAI_ERR_NO_DEVICE, "gpuai_net_create: no such CUDA device");
+  if (!encode_fn()) return err(GPUAI_ERR_CUDA, "gpuai_net_create: cuTensorMapEncodeTiled unavailable");
+  gpuai_net *net = new gpuai_net;
+  net->device = device;
+  auto fail = [&](int rc) {
+    gpuai_net_destroy(net);
+    return rc;
+  };
+  if (cudaSetDevice(device) != cudaSuccess) return fail(err(GPUAI_ERR_CUDA, "cudaSetDevice failed"));
+  // the GEMM's shared-memory ring needs the opt-in limit (set here, outside any stream capture)
+  if (cudaFuncSetAttribute(gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemLimit) != cudaSuccess)
+    return fail(err(GPUAI_ERR_CUDA, "gpuai_net_create: cannot enable 227 KiB shared memory for the GEMM kernel"));
+  const uint32_t L = round128(max_batch);
+  net->rows = L;
+  auto &A = net->allocs;
+  cudaError_t e = cudaStreamCreateWithFlags(&net->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = dalloc(A, &net->params, kParams);
+  if (e == cudaSuccess) e = dalloc(A, &net->adam_m, kParams);
+  if (e == cudaSuccess) e = dalloc(A, &net->adam_v, kParams);
+  if (e == cudaSuccess) e = dalloc(A, &net->grad, kParams);
+  if (e == cudaSuccess) e = dalloc(A, &net->gout, kParams);
+  if (e == cudaSuccess) e = dalloc(A, &net->W1b, (size_t)kH * kInPad);
+  if (e == cudaSuccess) e = dalloc(A, &net->W2b, (size_t)kH * kH);
+  if (e == cudaSuccess) e = dalloc(A, &net->W3b, (size_t)kOut * kH);
+  if (e == cudaSuccess) e = dalloc(A, &net->W2T, (size_t)kH * kH);
+  if (e == cudaSuccess) e = dalloc(A, &net->W3T, (size_t)kH * kOut);
+  if (e == cudaSuccess) e = fwd_alloc(net->fw, L, A);
+  if (e == cudaSuccess) e = dalloc(A, &net->Xt, (size_t)kInPad * L);
+  if (e == cudaSuccess) e = dalloc(A, &net->H1t, (size_t)kH * L);
+  if (e == cudaSuccess) e = dalloc(A, &net->H2t, (size_t)kH * L);
+  if (e == cudaSuccess) e = dalloc(A, &net->dZ3, (size_t)L * kOut);
+  if (e == cudaSuccess) e = dalloc(A, &net->dZ3t, (size_t)kOut * L);
+  if (e == cudaSuccess) e = dalloc(A, &net->dZ2, (size_t)L * kH);
+  if (e == cudaSuccess) e = dalloc(A, &net->dZ2t, (size_t)kH * L);
+  if (e == cudaSuccess) e = dalloc(A, &net->dZ1t, (size_t)kH * L);
+  if (e == cudaSuccess) e = dalloc(A, &net->dv, L);
+  if (e == cudaSuccess) e = dalloc(A, &net->rowloss, 2 * (size_t)L);
+  if (e == cudaSuccess) e = dalloc(A, &net->loss2, 2);
+  if (e == cudaSuccess) e = dalloc(A, &net->value, L);
+  if (e == cudaSuccess) e = dalloc(A, &net->p3, (size_t)kSplit3 * kOut * kH);
+  if (e == cudaSuccess) e = dalloc(A, &net->p2, (size_t)kSplit2 * kH * kH);
+  if (e == cudaSuccess) e = dalloc(A, &net->p1, (size_t)kSplit1 * kH * kInPad);
+  if (e == cudaSuccess) e = dalloc(A, &net->status, 1);
+  if (e == cudaSuccess) e = dalloc(A, &net->in_boards, L);
+  if (e == cudaSuccess) e = dalloc(A, &net->in_z, L);
+  if (e == cudaSuccess) e = dalloc(A, &net->in_q, (size_t)L * kMaxMoves);
+  if (e != cudaSuccess) return fail(cuda_err(e, "gpuai_net_create: allocation"));
+  e = make_map(&net->mW1, net->W1b, kH, kInPad, 256);
+  if (e == cudaSuccess) e = make_map(&net->mW2, net->W2b, kH, kH, 256);
+  if (e == cudaSuccess) e = make_map(&net->mW3, net->W3b, kOut, kH, 256);
+  if (e == cudaSuccess) e = make_map(&net->mW2T, net->W2T, kH, kH, 256);
+  if (e == cudaSuccess) e = make_map(&net->mW3T, net->W3T, kH, kOut, 256);
+  if (e == cudaSuccess) e = make_map(&net->mXt, net->Xt, kInPad, L, kInPad);
+  if (e == cudaSuccess) e = make_map(&net->mH1t, net->H1t, kH, L, 256);
+  if (e == cudaSuccess) e = make_map(&net->mH2t, net->H2t, kH, L, 256);
+  if (e == cudaSuccess) e = make_map(&net->mdZ3, net->dZ3, L, kOut, kBM);
+  if (e == cudaSuccess) e = make_map(&net->mdZ3t, net->dZ3t, kOut, L, kBM);
+  if (e == cudaSuccess) e = make_map(&net->mdZ2, net->dZ2, L, kH, kBM);
+  if (e == cudaSuccess) e = make_map(&net->mdZ2t, net->dZ2t, kH, L, kBM);
+  if (e == cudaSuccess) e = make_map(&net->mdZ1t, net->dZ1t, kH, L, kBM);
+  if (e != cudaSuccess) return fail(cuda_err(e, "gpuai_net_create: tensor maps"));
+  // the transposed activations are read up to the padded batch: start them at zero
+  e = cudaMemsetAsync(net->status, 0, sizeof(uint32_t), net->stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(net->Xt, 0, (size_t)kInPad * L * sizeof(bf16), net->stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(net->H1t, 0, (size_t)kH * L * sizeof(bf16), net->stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(net->H2t, 0, (size_t)kH * L * sizeof(bf16), net->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(net->stream);
+  if (e != cudaSuccess) return fail(cuda_err(e, "gpuai_net_create: clear"));
+  std::vector<float> p;
+  init_params(p, init_seed);
+  const int rc = gpuai_net_set_params(net, p.data());
+  if (rc) return fail(rc);
+  *out = net;
+  return GPUAI_OK;
+}
+
+void gpuai_net_destroy(gpuai_net *net) {
+  if (!net) return;
+  cudaSetDevice(net->device);
+  if (net->stream) cudaStreamSynchronize(net->stream);
+  for (void *p : net->allocs) cudaFree(p);
+  if (net->stream) cudaStreamDestroy(net->stream);
+  delete net;
+}
+
+int gpuai_net_get_params(gpuai_net *net, float *params) {
+  if (!net || !params) return err(GPUAI_ERR_INVALID, "gpuai_net_get_params: NULL");
+  std::lock_guard<std::mutex> lock(net->mu);
+  NCK(cudaSetDevice(net->device), "cudaSetDevice");
+  NCK(cudaMemcpyAsync(params, net->params, kParams * sizeof(float), cudaMemcpyDeviceToHost, net->stream), "D2H");
+  NCK(cudaStreamSynchronize(net->stream), "D2H");
+  return GPUAI_OK;
+}
+
+int gpuai_net_set_params(gpuai_net *net, const float *params) {
+  if (!net || !params) return err(GPUAI_ERR_INVALID, "gpuai_net_set_params: NULL");
+  std::lock_guard<std::mutex> lock(net->mu);
+  NCK(cudaSetDevice(net->device), "cudaSetDevice");
+  const cudaStream_t s = net->stream;
+  NCK(cudaMemcpyAsync(net->params, params, kParams * sizeof(float), cudaMemcpyHostToDevice, s), "H2D");
+  NCK(cudaMemsetAsync(net->adam_m, 0, kParams * sizeof(float), s), "clear Adam state");
+  NCK(cudaMemsetAsync(net->adam_v, 0, kParams * sizeof(float), s), "clear Adam state");
+  net->step = 0;
+  NCK(run_adam(net, 2, nullptr, 0.0f, s), "BF16 copies");
+  NCK(cudaStreamSynchronize(s), "set params");
+  return GPUAI_OK;
+}
+
+int gpuai_net_save(gpuai_net *net, const char *path) {
+  if (!net || !path) return err(GPUAI_ERR_INVALID, "gpuai_net_save: NULL");
+  std::lock_guard<std::mutex> lock(net->mu);
+  NCK(cudaSetDevice(net->device), "cudaSetDevice");
+  std::vector<float> buf(3 * kParams);
+  const cudaStream_t s = net->stream;
+  NCK(cudaMemcpyAsync(buf.data(), net->params, kParams * 4, cudaMemcpyDeviceToHost, s), "D2H");
+  NCK(cudaMemcpyAsync(buf.data() + kParams, net->adam_m, kParams * 4, cudaMemcpyDeviceToHost, s), "D2H");
+  NCK(cudaMemcpyAsync(buf.data() + 2 * kParams, net->adam_v, kParams * 4, cudaMemcpyDeviceToHost, s), "D2H");
+  NCK(cudaStreamSynchronize(s), "D2H");
+  Header h;
+  std::memset(&h, 0, sizeof h);
+  std::memcpy(h.magic, "GPUAINET", 8);
+  h.version = 1;
+  h.features = kIn;
+  h.in_pad = kInPad;
+  h.hidden = kH;
+  h.logits = kOut;
+  h.nparams = (uint32_t)kParams;
+  h.step = net->step;
+  FILE *f = std::fopen(path, "wb");
+  if (!f) return err(GPUAI_ERR_INVALID, std::string("gpuai_net_save: cannot open ") + path);
+  const bool ok = std::fwrite(&h, sizeof h, 1, f) == 1 && std::fwrite(buf.data(), 4, buf.size(), f) == buf.size();
+  const bool closed = std::fclose(f) == 0;
+  if (!ok || !closed) return err(GPUAI_ERR_INVALID, std::string("gpuai_net_save: write failed: ") + path);
+  return GPUAI_OK;
+}
+
+int gpuai_net_load(gpuai_net *net, const char *path) {
+  if (!net || !path) return err(GPUAI_ERR_INVALID, "gpuai_net_load: NULL");
+  FILE *f = std::fopen(path, "rb");
+  if (!f) return err(GPUAI_ERR_INVALID, std::string("gpuai_net_load: cannot open ") + path);
+  Header h;
+  std::vector<float> buf(3 * kParams);
+  const bool ok = std::fread(&h, sizeof h, 1, f) == 1 && std::fread(buf.data(), 4, buf.size(), f) == buf.size();
+  std::fclose(f);
+  if (!ok || std::memcmp(h.magic, "GPUAINET", 8) != 0 || h.version != 1 || h.features != kIn ||
+      h.in_pad != kInPad || h.hidden != kH || h.logits != kOut || h.nparams != kParams)
+    return err(GPUAI_ERR_INVALID, std::string("gpuai_net_load: not a network file of this layout: ") + path);
+  int rc = gpuai_net_set_params(net, buf.data());
+  if (rc) return rc;
+  std::lock_guard<std::mutex> lock(net->mu);
+  const cudaStream_t s = net->stream;
+  NCK(cudaMemcpyAsync(net->adam_m, buf.data() + kParams, kParams * 4, cudaMemcpyHostToDevice, s), "H2D");
+  NCK(cudaMemcpyAsync(net->adam_v, buf.data() + 2 * kParams, kParams * 4, cudaMemcpyHostToDevice, s), "H2D");
+  NCK(cudaStreamSynchronize(s), "H2D");
+  net->step = h.step;
+  return GPUAI_OK;
+}
+
+int gpuai_net_forward(gpuai_net *net, const gpuai_board *boards, uint32_t n, float *value, float *logits) {
+  if (!net || (n && (!boards || !value))) return err(GPUAI_ERR_INVALID, "gpuai_net_forward: NULL");
+  std::lock_guard<std::mutex> lock(net->mu);
+  NCK(cudaSetDevice(net->device), "cudaSetDevice");
+  const cudaStream_t s = net->stream;
+  for (uint32_t done = 0; done < n;) {
+    const uint32_t c = n - done < net->rows ? n - done : net->rows;
+    NCK(cudaMemcpyAsync(net->in_boards, boards + done, c * sizeof(gpuai_board), cudaMemcpyHostToDevice, s), "H2D");
+    NCK(forward(net, net->fw, net->in_boards, c, nullptr, net->status, s), "forward");
+    tanh_kernel<<<(c + 255) / 256, 256, 0, s>>>(net->fw.vraw, c, net->value);
+    NCK(cudaGetLastError(), "tanh");
+    NCK(cudaMemcpyAsync(value + done, net->value, c * sizeof(float), cudaMemcpyDeviceToHost, s), "D2H");
+    if (logits)
+      NCK(cudaMemcpyAsync(logits + (size_t)done * kOut, net->fw.logits, (size_t)c * kOut * sizeof(float),
+                          cudaMemcpyDeviceToHost, s),
+          "D2H");
+    const int rc = check_status(net);
+    if (rc) return rc;
+    done += c;
+  }
+  return GPUAI_OK;
+}
+
+int gpuai_net_gradients(gpuai_net *net, const gpuai_board *boards, const float *value_target, const float *move_q,
+                        uint32_t n, float tau, float value_coef, float *grads, float *loss2) {
+  if (!net || !boards || !value_target || !move_q || !grads) return err(GPUAI_ERR_INVALID, "gpuai_net_gradients: NULL");
+  if (n == 0 || n > net->rows) return err(GPUAI_ERR_INVALID, "gpuai_net_gradients: n outside 1..max_batch");
+  if (!(tau > 0.0f)) return err(GPUAI_ERR_INVALID, "gpuai_net_gradients: tau must be > 0");
+  std::lock_guard<std::mutex> lock(net->mu);
+  NCK(cudaSetDevice(net->device), "cudaSetDevice");
+  const cudaStream_t s = net->stream;
+  NCK(cudaMemcpyAsync(net->in_boards, boards, n * sizeof(gpuai_board), cudaMemcpyHostToDevice, s), "H2D");
+  NCK(cudaMemcpyAsync(net->in_z, value_target, n * sizeof(float), cudaMemcpyHostToDevice, s), "H2D");
+  NCK(cudaMemcpyAsync(net->in_q, move_q, (size_t)n * kMaxMoves * sizeof(float), cudaMemcpyHostToDevice, s), "H2D");
+  uint32_t splits[3];
+  NCK(backward_impl(net, net->in_boards, net->in_z, net->in_q, n, tau, value_coef, splits, s), "backward");
+  NCK(run_adam(net, 1, splits, 0.0f, s), "gradient gather");
+  NCK(cudaMemcpyAsync(grads, net->gout, kParams * sizeof(float), cudaMemcpyDeviceToHost, s), "D2H");
+  if (loss2) NCK(cudaMemcpyAsync(loss2, net->loss2, 2 * sizeof(float), cudaMemcpyDeviceToHost, s), "D2H");
+  return check_status(net);
+}
+
+int gpuai_net_train_step(gpuai_net *net, const gpuai_board *d_boards, const float *d_value_target,
+                         const float *d_move_q, uint32_t n, float lr, float tau, float value_coef, float *loss2) {
+  if (!net || !d_boards || !d_value_target || !d_move_q) return err(GPUAI_ERR_INVALID, "gpuai_net_train_step: NULL");
+  if (n == 0 || n > net->rows) return err(GPUAI_ERR_INVALID, "gpuai_net_train_step: n outside 1..max_batch");
+  if (!(tau > 0.0f) || !(lr >= 0.0f)) return err(GPUAI_ERR_INVALID, "gpuai_net_train_step: bad tau or lr");
+  std::lock_guard<std::mutex> lock(net->mu);
+  NCK(cudaSetDevice(net->device), "cudaSetDevice");
+  const cudaStream_t s = net->stream;
+  uint32_t splits[3];
+  NCK(backward_impl(net, d_boards, d_value_target, d_move_q, n, tau, value_coef, splits, s), "backward");
+  net->step++;
+  NCK(run_adam(net, 0, splits, lr, s), "adam");
+  if (loss2) {
+    NCK(cudaMemcpyAsync(loss2, net->loss2, 2 * sizeof(float), cudaMemcpyDeviceToHost, s), "D2H");
+    return check_status(net);
+  }
+  return GPUAI_OK;
+}
+
+int gpuai_label_positions(gpuai_ctx *ctx, const gpuai_board *d_pos, uint32_t n, uint32_t playouts_per_position,
+                          uint64_t seed, uint64_t stream_base, int32_t policy, float *d_value, float *d_move_q,
+                          uint8_t *d_nmoves, void *stream) {
+  if (!ctx) return err(GPUAI_ERR_INVALID, "gpuai_label_positions: ctx is NULL");
+  if (n == 0) return GPUAI_OK;
+  if (!d_pos || !d_value || !d_move_q || !d_nmoves) return err(GPUAI_ERR_INVALID, "gpuai_label_positions: NULL");
+  const uint32_t P = playouts_per_position;
+  if (P < kMaxMoves) return err(GPUAI_ERR_INVALID, "gpuai_label_positions: playouts_per_position must be >= 32");
+  if ((uint64_t)n * P >= 0x7fffffffull || (uint64_t)n * kLabelSlots >= 0x7fffffffull)
+    return err(GPUAI_ERR_INVALID, "gpuai_label_positions: n * playouts_per_position must stay below 2^31");
+  const cudaStream_t s = static_cast<cudaStream_t>(stream);
+  ga::Board *children = nullptr;
+  uint32_t *offsets = nullptr;
+  int8_t *out = nullptr;
+  const size_t nc = (size_t)n * kLabelSlots;
+  NCK(cudaMallocAsync(reinterpret_cast<void **>(&children), nc * sizeof(ga::Board), s), "label scratch");
+  cudaError_t e = cudaMallocAsync(reinterpret_cast<void **>(&offsets), (nc + 1) * sizeof(uint32_t), s);
+  if (e == cudaSuccess) e = cudaMallocAsync(reinterpret_cast<void **>(&out), (size_t)n * P, s);
+  int rc = GPUAI_OK;
+  if (e != cudaSuccess) {
+    rc = cuda_err(e, "label scratch");
+  } else {
+    label_children_kernel<<<(n + 127) / 128, 128, 0, s>>>(d_pos, n, P, children, offsets, d_nmoves);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) rc = cuda_err(e, "label children");
+  }
+  if (rc == GPUAI_OK)
+    rc = gpuai_playouts_device(ctx, reinterpret_cast<const gpuai_board *>(children), offsets, (uint32_t)nc, 0,
+                               n * P, seed, stream_base, policy, out, stream);
+  if (rc == GPUAI_OK) {
+    label_reduce_kernel<<<(n + 3) / 4, 128, 0, s>>>(d_pos, out, offsets, d_nmoves, n, P, d_value, d_move_q);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) rc = cuda_err(e, "label reduce");
+  }
+  if (out) cudaFreeAsync(out, s);
+  if (offsets) cudaFreeAsync(offsets, s);
+  if (children) cudaFreeAsync(children, s);
+  return rc;
+}
+
+}  // extern "C"

@@ -17,10 +17,17 @@
 //                    of the warp take one frontier node each
 //   playout_kernel   the playout kernel on the leaf boards (sizes and stream
 //                    ids read from device memory)
-//   backprop_kernel  one thread per leaf: visits and score up the path,
-//                    virtual loss removed
+//   backprop_kernel  one thread per leaf: visits and score up the path
 //
-// The four launches are replayed as one CUDA graph per step.  Because each
+// Learned searches (a policy/value network attached) add, between the
+// playouts and the backpropagation, the network's forward pass on the leaf
+// boards (net.cu) and leaf_eval_kernel, which turns a leaf's move logits into
+// priors of its moves and its value head into the leaf value.  Their selection
+// splits a node's slots by PUCT with virtual visits (split_puct) and expands a
+// node once it has been evaluated; backprop blends the network value with the
+// playout results.
+//
+// The launches of a step are replayed as one CUDA graph.  Because each
 // search is selected by a single warp in a fixed order and its playouts use
 // its own stream ids, a search's tree and result do not depend on which other
 // searches share the steps.
@@ -31,7 +38,10 @@
 #include "../../include/gpuai.h"
 #include "host/state.hpp"
 #include "launch.h"
+#include "net.h"
 #include "rules.cuh"
+
+#include <cuda_fp16.h>
 
 #include <cuda_runtime.h>
 
@@ -47,19 +57,23 @@
 namespace ga {
 namespace {
 
-constexpr uint32_t kExpanded = 1u, kTerminal = 2u;
+constexpr uint32_t kExpanded = 1u, kTerminal = 2u, kEvaluated = 4u;  // node state bits (info.y >> 16)
 constexpr int kMaxSelectDepth = 512;
 constexpr uint32_t kStatusSelectDepth = 8u;
 constexpr uint32_t kSelectWarps = 4;   // searches per select block
 constexpr uint32_t kMaxLeavesPerStep = 256;  // frontier capacity per search
 constexpr float kUcbC = 1.41421356f;
 constexpr int kMaxChildren = 64;  // moves per position handled by split_slots
+constexpr uint32_t kUnits = 64;   // learned searches: visit units per leaf slot (score2 = units * (1 + value))
+constexpr uint32_t kPriors = 32;  // stored priors per node (more moves: uniform priors)
+constexpr float kFpuReduction = 0.1f;  // unvisited child's Q = parent's Q - this
 
 struct Pool {  // one entry per node
   uint4 *info;   // {first child, nchild | state << 16, visits, score2}
   uint4 *board;
   int32_t *parent;
   uint32_t *move, *removed;
+  __half *prior;  // learned searches: kPriors per node, the node's moves' priors
 };
 
 struct Table {  // one entry per search slot
@@ -74,6 +88,12 @@ struct Leaves {
   unsigned long long *stream;
   int8_t *out;
   uint32_t *sizes;  // {leaves, playouts}
+  float *value;     // learned searches: network value for the side to move at the leaf
+};
+
+struct Learned {
+  float c_puct;
+  float value_weight;
 };
 
 __device__ __forceinline__ bool board_terminal(const Board &b) {
@@ -206,12 +226,53 @@ __device__ void split_slots(const Pool &p, int32_t first, int k, uint32_t parent
     if (give[c]) emit(first + c, give[c]);
 }
 
+// Learned searches: splits T slots over the k children of node n one slot at
+// a time, each to the child with the largest Q + c_puct * P * sqrt(N + t + 1)
+// / (1 + n + slots already given) (first on ties), where Q is the child's mean
+// score for the player to move at n (an unvisited child: n's own Q minus
+// kFpuReduction), P its prior (uniform when n has more than kPriors moves or
+// has not been evaluated), N = n's visits and n the child's, in leaf slots.
+template <class Emit>
+__device__ void split_puct(const Pool &p, int32_t n, int32_t first, int k, uint32_t parent_visits,
+                           uint32_t parent_score2, uint32_t st, uint32_t T, float c_puct, Emit &&emit) {
+  float q[kMaxChildren], pr[kMaxChildren], nv[kMaxChildren];
+  const bool priors = (st & kEvaluated) && k <= (int)kPriors;
+  const float fpu = parent_visits ? fmaxf(0.0f, 1.0f - 0.5f * (float)parent_score2 / (float)parent_visits -
+                                                    kFpuReduction)
+                                  : 0.5f;
+  for (int c = 0; c < k; c++) {
+    const uint4 ci = p.info[first + c];
+    q[c] = ci.z ? 0.5f * (float)ci.w / (float)ci.z : fpu;
+    nv[c] = (float)(ci.z / kUnits);
+    pr[c] = priors ? __half2float(p.prior[(size_t)n * kPriors + c]) : 1.0f / (float)k;
+  }
+  const float N = (float)(parent_visits / kUnits);
+  uint32_t give[kMaxChildren];
+  for (int c = 0; c < k; c++) give[c] = 0;
+  for (uint32_t t = 0; t < T; t++) {
+    const float sq = c_puct * sqrtf(N + (float)t + 1.0f);
+    int best = 0;
+    float bs = -3.0e38f;
+    for (int c = 0; c < k; c++) {
+      const float sc = q[c] + sq * pr[c] / (1.0f + nv[c] + (float)give[c]);
+      if (sc > bs) {
+        bs = sc;
+        best = c;
+      }
+    }
+    give[best]++;
+  }
+  for (int c = 0; c < k; c++)
+    if (give[c]) emit(first + c, give[c]);
+}
+
 // One warp per search.  The frontier holds (node, slots) pairs; each round
 // every lane takes frontier entries, expands or splits them, and the warp
 // compacts the children it produced into the next frontier and the leaf
 // slots it produced into the search's output range.
+template <bool LEARNED>
 __global__ void __launch_bounds__(32 * kSelectWarps) select_kernel(Pool p, Table t, Leaves l, uint32_t slots,
-                                                                   uint32_t ppl, uint32_t *status) {
+                                                                   uint32_t ppl, Learned lrn, uint32_t *status) {
   __shared__ int32_t f_node[kSelectWarps][2][kMaxLeavesPerStep];
   __shared__ uint32_t f_cnt[kSelectWarps][2][kMaxLeavesPerStep];
   const uint32_t lane = threadIdx.x & 31u, wi = threadIdx.x >> 5;
@@ -240,7 +301,7 @@ __global__ void __launch_bounds__(32 * kSelectWarps) select_kernel(Pool p, Table
       const uint32_t e = base + lane;
       // pass 1: what each lane's entry produces (children entries or leaf slots)
       int32_t n = -1, first = 0, k = 0;
-      uint32_t T = 0, leaf = 0, kids = 0, visits = 0, st = 0;
+      uint32_t T = 0, leaf = 0, kids = 0, visits = 0, score2 = 0, st = 0;
       int grow = 0;  // children this lane's node gets if it is expanded now
       if (e < nf) {
         n = f_node[wi][cur][e];
@@ -248,13 +309,20 @@ __global__ void __launch_bounds__(32 * kSelectWarps) select_kernel(Pool p, Table
         const uint4 inf = p.info[n];
         st = inf.y >> 16;
         visits = inf.z;
+        score2 = inf.w;
         first = (int32_t)inf.x;
         k = (int32_t)(inf.y & 0xffffu);
         if (st & kTerminal) leaf = T;
         else if (!(st & kExpanded)) {
-          if (T == 1) leaf = 1;
-          else grow = child_count(p, n);
-          if (T > 1 && grow == 0) leaf = T;
+          if (LEARNED) {
+            // a node is expanded once the network has evaluated it
+            if (st & kEvaluated) grow = child_count(p, n);
+            if (grow == 0) leaf = T;
+          } else {
+            if (T == 1) leaf = 1;
+            else grow = child_count(p, n);
+            if (T > 1 && grow == 0) leaf = T;
+          }
         }
       }
       // node indices for this round's expansions, in lane order; an expansion
@@ -274,8 +342,11 @@ __global__ void __launch_bounds__(32 * kSelectWarps) select_kernel(Pool p, Table
         leaf = T;
       }
       node_next += (int32_t)fit_end;
-      if (e < nf) {
-        if (!leaf) split_slots(p, first, k, visits, T, [&](int32_t, uint32_t) { kids++; });
+      if (e < nf && !leaf) {
+        if (LEARNED)
+          split_puct(p, n, first, k, visits, score2, st, T, lrn.c_puct, [&](int32_t, uint32_t) { kids++; });
+        else
+          split_slots(p, first, k, visits, T, [&](int32_t, uint32_t) { kids++; });
       }
       __syncwarp();
       // warp prefix sums of children entries and leaf slots
@@ -302,11 +373,13 @@ __global__ void __launch_bounds__(32 * kSelectWarps) select_kernel(Pool p, Table
           }
         } else {
           uint32_t w = kid_at;
-          split_slots(p, first, k, visits, T, [&](int32_t child, uint32_t cnt) {
+          auto put = [&](int32_t child, uint32_t cnt) {
             f_node[wi][cur ^ 1][w] = child;
             f_cnt[wi][cur ^ 1][w] = cnt;
             w++;
-          });
+          };
+          if (LEARNED) split_puct(p, n, first, k, visits, score2, st, T, lrn.c_puct, put);
+          else split_slots(p, first, k, visits, T, put);
         }
       }
       __syncwarp();
@@ -343,6 +416,83 @@ __global__ void backprop_kernel(Pool p, Table t, Leaves l, uint32_t ppl, uint32_
   }
   (void)root;
   atomicAdd(&t.done[s], (unsigned long long)ppl);
+}
+
+// Learned searches: one thread per leaf; the leaf's result for PLAYER_1 is
+// value_weight * network value + (1 - value_weight) * playout mean (terminal
+// leaves: the playouts, which end at once with the exact result), added as
+// kUnits visits.
+__global__ void backprop_learned_kernel(Pool p, Table t, Leaves l, uint32_t ppl, uint32_t max_leaves,
+                                        Learned lrn) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= max_leaves || i >= l.sizes[0]) return;
+  const int32_t s = l.search[i];
+  const int32_t leaf = l.node[i];
+  int sum = 0;  // outcomes for PLAYER_1
+  for (uint32_t k = 0; k < ppl; k++) sum += l.out[(size_t)i * ppl + k];
+  const float pm = (float)sum / (float)ppl;
+  float x1 = pm;
+  if (!((p.info[leaf].y >> 16) & kTerminal)) {
+    const float v1 = (p.board[leaf].w & 1u) ? -l.value[i] : l.value[i];  // value is for the side to move
+    x1 = lrn.value_weight * v1 + (1.0f - lrn.value_weight) * pm;
+  }
+  x1 = fminf(1.0f, fmaxf(-1.0f, x1));
+  const uint32_t s1 = (uint32_t)lrintf((float)kUnits * (1.0f + x1));  // half points of PLAYER_1
+  const uint32_t s2 = 2u * kUnits - s1;
+  for (int32_t n = leaf; n >= 0; n = p.parent[n]) {
+    const uint32_t mover = (p.board[n].w & 1u) ^ 1u;  // 0: PLAYER_1 moved into n
+    atomicAdd(&p.info[n].z, kUnits);
+    atomicAdd(&p.info[n].w, mover == 0 ? s1 : s2);
+  }
+  atomicAdd(&t.done[s], (unsigned long long)ppl);
+}
+
+// Learned searches: one thread per leaf.  The leaf value (tanh of the value
+// head, for the side to move) and, the first time a node is a leaf, its
+// moves' priors: the softmax of the move logits over its legal (from, to)
+// pairs, a pair's probability shared equally by the moves that have it.
+__global__ void leaf_eval_kernel(Pool p, Leaves l, const float *logits, const float *vraw, uint32_t max_leaves) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= max_leaves || i >= l.sizes[0]) return;
+  l.value[i] = tanhf(vraw[i]);
+  const int32_t n = l.node[i];
+  const uint32_t st = p.info[n].y >> 16;
+  if (st & (kEvaluated | kTerminal)) return;
+  const uint4 bv = l.board[i];
+  const Board b{bv.x, bv.y, bv.z, bv.w};
+  Side sd;
+  make_side(b, sd);
+  const uint32_t J = jumpers(sd);
+  const int k = count_moves(sd, J);
+  if (k >= 1 && k <= (int)kPriors) {
+    uint16_t pair[kPriors] = {};
+    uint8_t of[kPriors];
+    uint8_t mult[kPriors];
+    int np = 0, m = 0;
+    for_each_move(sd, J, [&](int from, int to, uint32_t, int, uint32_t) {
+      const uint16_t pi = (uint16_t)(from * 32 + to);
+      int u = 0;
+      while (u < np && pair[u] != pi) u++;
+      if (u == np) {
+        pair[np] = pi;
+        mult[np] = 0;
+        np++;
+      }
+      mult[u]++;
+      of[m++] = (uint8_t)u;
+      return false;
+    });
+    const float *lr = logits + (size_t)i * net::kOut;
+    float lmax = -3.0e38f;
+    for (int u = 0; u < np; u++) lmax = fmaxf(lmax, lr[pair[u]]);
+    float sum = 0.0f;
+    for (int u = 0; u < np; u++) sum += expf(lr[pair[u]] - lmax);
+    for (int j = 0; j < k; j++) {
+      const int u = of[j];
+      p.prior[(size_t)n * kPriors + j] = __float2half(expf(lr[pair[u]] - lmax) / sum / (float)mult[u]);
+    }
+  }
+  atomicOr(&p.info[n].y, kEvaluated << 16);
 }
 
 __global__ void init_search_kernel(Pool p, Table t, int32_t slot, int32_t start, int32_t cap, uint4 board,
@@ -385,6 +535,10 @@ struct gpuai_searches {
   uint32_t graph_q = 0;
   std::mutex mu;
   std::vector<void *> allocations;
+  // learned searches
+  gpuai_net *net = nullptr;
+  Learned lrn{1.5f, 1.0f};
+  ga::net::Fwd fw;
 };
 
 namespace {
@@ -418,8 +572,13 @@ int enqueue_step(gpuai_searches *s, uint32_t q) {
   // until poll reads them
   SCK(cudaMemsetAsync(s->ctl, 0, sizeof(uint32_t), st), "reset work counter");
   quota_kernel<<<1, 1024, 0, st>>>(s->tab, s->slots, q, s->ppl, s->leaves);
-  select_kernel<<<(s->slots + kSelectWarps - 1) / kSelectWarps, 32 * kSelectWarps, 0, st>>>(
-      s->pool, s->tab, s->leaves, s->slots, s->ppl, s->ctl + 1);
+  const uint32_t sel_blocks = (s->slots + kSelectWarps - 1) / kSelectWarps;
+  if (s->net)
+    select_kernel<true><<<sel_blocks, 32 * kSelectWarps, 0, st>>>(s->pool, s->tab, s->leaves, s->slots, s->ppl,
+                                                                   s->lrn, s->ctl + 1);
+  else
+    select_kernel<false><<<sel_blocks, 32 * kSelectWarps, 0, st>>>(s->pool, s->tab, s->leaves, s->slots, s->ppl,
+                                                                    s->lrn, s->ctl + 1);
   PlayoutArgs a;
   a.pos = reinterpret_cast<const Board *>(s->leaves.board);
   a.offsets = nullptr;
@@ -436,7 +595,17 @@ int enqueue_step(gpuai_searches *s, uint32_t q) {
   a.dev_sizes = s->leaves.sizes;
   SCK(launch_playouts(a, s->policy, kPlayoutBlock, s->sms * s->blocks_per_sm, st), "playout kernel launch");
   const uint32_t max_leaves = s->slots * s->qmax;
-  backprop_kernel<<<(max_leaves + 255) / 256, 256, 0, st>>>(s->pool, s->tab, s->leaves, s->ppl, max_leaves);
+  if (s->net) {
+    SCK(ga::net::forward(s->net, s->fw, reinterpret_cast<const gpuai_board *>(s->leaves.board), 0, s->leaves.sizes,
+                         s->ctl + 1, st),
+        "network forward on the leaves");
+    leaf_eval_kernel<<<(max_leaves + 255) / 256, 256, 0, st>>>(s->pool, s->leaves, s->fw.logits, s->fw.vraw,
+                                                               max_leaves);
+    backprop_learned_kernel<<<(max_leaves + 255) / 256, 256, 0, st>>>(s->pool, s->tab, s->leaves, s->ppl,
+                                                                      max_leaves, s->lrn);
+  } else {
+    backprop_kernel<<<(max_leaves + 255) / 256, 256, 0, st>>>(s->pool, s->tab, s->leaves, s->ppl, max_leaves);
+  }
   SCK(cudaGetLastError(), "search kernel launch");
   return GPUAI_OK;
 }
@@ -628,6 +797,30 @@ int gpuai_searches_poll(gpuai_searches *s, uint64_t *done, uint64_t *budget, uin
     if (s->start[i] < 0) done[i] = budget[i] = 0;
   if (status) *status = st;
   if (st) return err(GPUAI_ERR_LIMIT, "gpuai_searches_poll: a kernel reported a limit");
+  return GPUAI_OK;
+}
+
+int gpuai_searches_set_net(gpuai_searches *s, gpuai_net *net, float value_weight, float c_puct) {
+  if (!s) return err(GPUAI_ERR_INVALID, "gpuai_searches_set_net: NULL");
+  if (!(value_weight >= 0.0f && value_weight <= 1.0f) || !(c_puct > 0.0f && c_puct < 1.0e6f))
+    return err(GPUAI_ERR_INVALID, "gpuai_searches_set_net: value_weight must be in [0, 1] and c_puct > 0");
+  std::lock_guard<std::mutex> lock(s->mu);
+  for (uint32_t i = 0; i < s->slots; i++)
+    if (s->start[i] >= 0) return err(GPUAI_ERR_INVALID, "gpuai_searches_set_net: searches are admitted");
+  if (net && ga::net::device_of(net) != s->device)
+    return err(GPUAI_ERR_INVALID, "gpuai_searches_set_net: network and searches are on different devices");
+  SCK(cudaSetDevice(s->device), "cudaSetDevice");
+  if (net && !s->pool.prior) {
+    const size_t L = (size_t)s->slots * s->qmax;
+    SCK(dalloc(s, &s->pool.prior, (size_t)s->pool_nodes * kPriors), "prior pool");
+    SCK(dalloc(s, &s->leaves.value, L), "leaf values");
+    SCK(ga::net::fwd_alloc(s->fw, (uint32_t)L, s->allocations), "network workspace");
+  }
+  s->net = net;
+  s->lrn.c_puct = c_puct;
+  s->lrn.value_weight = value_weight;
+  if (s->graph) cudaGraphExecDestroy(s->graph);  // the step's launches change
+  s->graph = nullptr;
   return GPUAI_OK;
 }
 

@@ -92,8 +92,25 @@ def load_library(path: str = LIB_PATH):
     lib.gpuai_searches_poll.argtypes = [ctypes.c_void_p, _u64p, _u64p, ctypes.c_uint32, _u32p]
     lib.gpuai_searches_children.argtypes = [ctypes.c_void_p, ctypes.c_int32, _u8p, _u32p, _u32p, ctypes.c_uint32,
                                             _u32p, _u32p]
+    _f32p = ctypes.POINTER(ctypes.c_float)
+    vp = ctypes.c_void_p
+    lib.gpuai_net_create.argtypes = [ctypes.c_int, ctypes.c_uint32, ctypes.c_uint64, ctypes.POINTER(vp)]
+    lib.gpuai_net_destroy.argtypes = [vp]
+    lib.gpuai_net_destroy.restype = None
+    lib.gpuai_net_get_params.argtypes = [vp, _f32p]
+    lib.gpuai_net_set_params.argtypes = [vp, _f32p]
+    lib.gpuai_net_save.argtypes = [vp, ctypes.c_char_p]
+    lib.gpuai_net_load.argtypes = [vp, ctypes.c_char_p]
+    lib.gpuai_net_forward.argtypes = [vp, _u32p, ctypes.c_uint32, _f32p, _f32p]
+    lib.gpuai_net_gradients.argtypes = [vp, _u32p, _f32p, _f32p, ctypes.c_uint32, ctypes.c_float, ctypes.c_float,
+                                        _f32p, _f32p]
+    lib.gpuai_net_train_step.argtypes = [vp, vp, vp, vp, ctypes.c_uint32, ctypes.c_float, ctypes.c_float,
+                                         ctypes.c_float, _f32p]
+    lib.gpuai_label_positions.argtypes = [vp, vp, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_uint64,
+                                          ctypes.c_int32, vp, vp, vp, vp]
+    lib.gpuai_searches_set_net.argtypes = [vp, vp, ctypes.c_float, ctypes.c_float]
     for name in header_symbols():
-        if name not in ("gpuai_last_error", "gpuai_destroy", "gpuai_searches_destroy"):
+        if name not in ("gpuai_last_error", "gpuai_destroy", "gpuai_searches_destroy", "gpuai_net_destroy"):
             getattr(lib, name).restype = ctypes.c_int
     _lib = lib
     return lib
@@ -184,6 +201,12 @@ class Engine:
         _check(self.lib.gpuai_random_positions(self.ctx, seed, n, min_plies, max_plies, out.ctypes.data_as(_u32p)))
         return out
 
+    def label_positions(self, d_pos: int, n: int, playouts_per_position: int, seed: int, stream_base: int,
+                        policy: int, d_value: int, d_move_q: int, d_nmoves: int, stream: Optional[int] = None):
+        """Enqueue GPU-playout training labels for n device boards (gpuai_label_positions)."""
+        _check(self.lib.gpuai_label_positions(self.ctx, d_pos, n, playouts_per_position, seed, stream_base, policy,
+                                              d_value, d_move_q, d_nmoves, stream))
+
     def set_launch(self, policy: int, block_threads: int, blocks_per_sm: int = 0):
         _check(self.lib.gpuai_set_launch(self.ctx, policy, block_threads, blocks_per_sm))
 
@@ -263,6 +286,11 @@ class Searches:
         k = min(n.value, max_children)
         return {"moves": moves[:k], "visits": visits[:k], "score2": score2[:k], "nodes": used.value}
 
+    def set_net(self, net: Optional["Net"], value_weight: float = 1.0, c_puct: float = 1.5):
+        """Evaluate leaves with `net` (None: plain playout searches)."""
+        _check(self.lib.gpuai_searches_set_net(self.h, net.h if net is not None else None, value_weight, c_puct))
+        self.net = net  # keep the network alive while the searches use it
+
     def best(self, slot: int):
         """Most visited root move (None for a finished game) and the child statistics."""
         c = self.children(slot)
@@ -270,3 +298,83 @@ class Searches:
             return None, c
         i = int(np.argmax(c["visits"]))
         return c["moves"][i], c
+
+
+NET_FEATURES = 129
+NET_HIDDEN = 256
+NET_LOGITS = 1024
+NET_MAX_MOVES = 32
+NET_PARAMS = 378625
+
+
+class Net:
+    """Policy/value network (gpuai_net_*): BF16 tensor-core forward, backward and Adam."""
+
+    def __init__(self, device: int = 0, max_batch: int = 8192, seed: int = 0):
+        self.lib = load_library()
+        h = ctypes.c_void_p()
+        _check(self.lib.gpuai_net_create(device, max_batch, seed, ctypes.byref(h)))
+        self.h = h
+        self.max_batch = max_batch
+
+    def close(self):
+        if self.h:
+            self.lib.gpuai_net_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def params(self) -> np.ndarray:
+        p = np.zeros(NET_PARAMS, np.float32)
+        _check(self.lib.gpuai_net_get_params(self.h, p.ctypes.data_as(ctypes.POINTER(ctypes.c_float))))
+        return p
+
+    def set_params(self, p):
+        a = np.ascontiguousarray(p, dtype=np.float32)
+        if a.shape != (NET_PARAMS,):
+            raise ValueError(f"expected {NET_PARAMS} parameters")
+        _check(self.lib.gpuai_net_set_params(self.h, a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))))
+
+    def save(self, path: str):
+        _check(self.lib.gpuai_net_save(self.h, os.fsencode(path)))
+
+    def load(self, path: str):
+        _check(self.lib.gpuai_net_load(self.h, os.fsencode(path)))
+
+    def forward(self, boards, want_logits: bool = True):
+        """(value for the side to move, n x 1024 logits or None)."""
+        b = _boards(boards)
+        n = b.shape[0]
+        fp = ctypes.POINTER(ctypes.c_float)
+        value = np.zeros(n, np.float32)
+        logits = np.zeros((n, NET_LOGITS), np.float32) if want_logits else None
+        _check(self.lib.gpuai_net_forward(self.h, b.ctypes.data_as(_u32p), n, value.ctypes.data_as(fp),
+                                          logits.ctypes.data_as(fp) if logits is not None else None))
+        return value, logits
+
+    def gradients(self, boards, value_target, move_q, tau: float = 0.1, value_coef: float = 1.0):
+        """(gradient in parameter order, [policy loss, value loss]) without updating."""
+        b = _boards(boards)
+        n = b.shape[0]
+        fp = ctypes.POINTER(ctypes.c_float)
+        z = np.ascontiguousarray(value_target, np.float32)
+        q = np.ascontiguousarray(move_q, np.float32).reshape(n, NET_MAX_MOVES)
+        g = np.zeros(NET_PARAMS, np.float32)
+        loss = np.zeros(2, np.float32)
+        _check(self.lib.gpuai_net_gradients(self.h, b.ctypes.data_as(_u32p), z.ctypes.data_as(fp),
+                                            q.ctypes.data_as(fp), n, tau, value_coef, g.ctypes.data_as(fp),
+                                            loss.ctypes.data_as(fp)))
+        return g, loss
+
+    def train_step(self, d_boards: int, d_value: int, d_move_q: int, n: int, lr: float, tau: float = 0.1,
+                   value_coef: float = 1.0, want_loss: bool = False):
+        """One Adam step on device rows; returns [policy, value] loss when want_loss (waits)."""
+        loss = np.zeros(2, np.float32) if want_loss else None
+        _check(self.lib.gpuai_net_train_step(self.h, d_boards, d_value, d_move_q, n, lr, tau, value_coef,
+                                             loss.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+                                             if loss is not None else None))
+        return loss

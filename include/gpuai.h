@@ -118,11 +118,12 @@ int gpuai_get_launch(gpuai_ctx *ctx, int32_t policy, int32_t *block_threads, int
  * Replaces the reference's one-search-per-MCTSPlayer loop
  * (src/player.cpp:134-150, src/mcts.cpp:63-191) with searches whose UCT trees
  * live in one node pool in device memory.  One step advances every active
- * search: up to `leaves_per_search` UCT descents with virtual loss per search
- * (leaves expanded the second time they are reached), playouts_per_leaf GPU
- * playouts per leaf, and backpropagation; the step's four kernels can be
- * replayed as a CUDA graph.  A search's result does not depend on the other
- * searches it shares steps with.  Best move = most visited root child. */
+ * search: `leaves_per_search` leaf slots per search are split over its tree
+ * level by level with the reference's GameTree::select rule (a leaf given
+ * more than one slot is expanded), playouts_per_leaf GPU playouts per leaf,
+ * and backpropagation; the step's kernels can be replayed as a CUDA graph.
+ * A search's result does not depend on the other searches it shares steps
+ * with.  Best move = most visited root child. */
 typedef struct gpuai_searches gpuai_searches;
 
 /* pool_nodes: node capacity of the shared pool (52 bytes of device memory per
@@ -145,6 +146,76 @@ int gpuai_searches_poll(gpuai_searches *s, uint64_t *done, uint64_t *budget, uin
  * score in half points for the player to move at the root. */
 int gpuai_searches_children(gpuai_searches *s, int32_t slot, gpuai_move *moves, uint32_t *visits,
                             uint32_t *score2, uint32_t max_children, uint32_t *nchildren, uint32_t *nodes_used);
+
+/* ---- policy/value network ----
+ * No counterpart in the reference (its only evaluation is the material
+ * heuristic, src/heuristic.cu:20-49).  A BF16 MLP on the tensor cores with FP32
+ * accumulation: 129 input features (side to move's men, its kings, the
+ * opponent's men, its kings, 32 squares each, then 1 if PLAYER_2 is to move),
+ * two hidden layers of 256 ReLU units, 1024 move logits (index from*32 + to,
+ * masked to the legal moves by the caller) and a tanh value for the side to
+ * move.  Parameters, FP32, in this order (GPUAI_NET_PARAMS floats):
+ *   W1[256][192] (input features 129..191 are zero padding), b1[256],
+ *   W2[256][256], b2[256], W3[1024][256], b3[1024], wv[256], bv[1].
+ * Forward, backward and Adam run as the library's own kernels; the GEMMs use
+ * BF16 copies of W1..W3 and BF16 activations.  Training targets per position:
+ * the value z for the side to move in [-1, 1], and move_q[32]: the value of
+ * each legal move (reference move-list order) for the side to move; the
+ * policy target is softmax(move_q / tau) over the legal moves.  Loss per
+ * position = cross entropy(policy target, masked softmax of the logits)
+ * + value_coef * (tanh value - z)^2, averaged over the batch.  Positions with
+ * more than GPUAI_NET_MAX_MOVES legal moves train the value only. */
+#define GPUAI_NET_FEATURES 129
+#define GPUAI_NET_HIDDEN 256
+#define GPUAI_NET_LOGITS 1024
+#define GPUAI_NET_MAX_MOVES 32
+#define GPUAI_NET_PARAMS 378625
+typedef struct gpuai_net gpuai_net;
+
+/* Parameters initialised uniformly in +-sqrt(6 / (fan_in + fan_out)) from
+ * Philox stream (init_seed), biases 0; max_batch = largest training batch. */
+int gpuai_net_create(int device, uint32_t max_batch, uint64_t init_seed, gpuai_net **out);
+void gpuai_net_destroy(gpuai_net *net);
+/* Host copies of the FP32 parameters; set_params also clears Adam's state. */
+int gpuai_net_get_params(gpuai_net *net, float *params);
+int gpuai_net_set_params(gpuai_net *net, const float *params);
+/* Parameters and Adam state as little-endian FP32 after a 64-byte header. */
+int gpuai_net_save(gpuai_net *net, const char *path);
+int gpuai_net_load(gpuai_net *net, const char *path);
+/* Forward pass on host boards: value[n] = tanh value for the side to move;
+ * logits (optional) = n x 1024 raw move logits. */
+int gpuai_net_forward(gpuai_net *net, const gpuai_board *boards, uint32_t n, float *value, float *logits);
+/* Gradients of the loss (host buffers, n <= max_batch) without an update:
+ * grads[GPUAI_NET_PARAMS] in parameter order; loss2 = {policy, value} means. */
+int gpuai_net_gradients(gpuai_net *net, const gpuai_board *boards, const float *value_target,
+                        const float *move_q, uint32_t n, float tau, float value_coef, float *grads,
+                        float *loss2);
+/* One Adam step (beta1 0.9, beta2 0.999, eps 1e-8) on device-resident
+ * training rows d_boards[n], d_value_target[n], d_move_q[n*32], enqueued on the
+ * net's stream.  loss2 (host, optional) makes the call wait and return the
+ * step's mean policy and value losses. */
+int gpuai_net_train_step(gpuai_net *net, const gpuai_board *d_boards, const float *d_value_target,
+                         const float *d_move_q, uint32_t n, float lr, float tau, float value_coef, float *loss2);
+/* Training labels from GPU playouts, on device buffers: for each position,
+ * each legal move m gets playouts_per_position / k (+1 for the first
+ * playouts_per_position % k moves) playouts of `policy` from the position after
+ * m; d_move_q[i*32 + m] = their mean outcome for the side to move at position
+ * i, d_value[i] = the mean over all its playouts (a random first move then
+ * playouts: the same estimate as that many playouts from position i).
+ * d_nmoves[i] = k, or 0 when the game is over or k > 32 (values then 0).
+ * Playout j of position i uses stream id stream_base + i * playouts_per_position
+ * + j under `seed`.  Enqueued on `stream` (NULL = legacy default stream);
+ * n * playouts_per_position must stay below 2^31. */
+int gpuai_label_positions(gpuai_ctx *ctx, const gpuai_board *d_pos, uint32_t n, uint32_t playouts_per_position,
+                          uint64_t seed, uint64_t stream_base, int32_t policy, float *d_value, float *d_move_q,
+                          uint8_t *d_nmoves, void *stream);
+/* Learned searches: leaves are also evaluated by `net` (NULL turns it off).
+ * Each leaf's value is value_weight * net value + (1 - value_weight) * its
+ * playout mean; a node's moves get the net's softmax over its legal moves as
+ * priors once it has been a leaf, and slots are split with PUCT
+ * (Q + c_puct * P * sqrt(N) / (1 + n)) instead of UCB1.  The net must not be
+ * trained while searches use it. */
+int gpuai_searches_set_net(gpuai_searches *s, gpuai_net *net, float value_weight, float c_puct);
 
 /* Playouts that allocate no device memory, for callers that may not call
  * cudaMalloc: for example a search server that reserves the whole device
