@@ -190,7 +190,7 @@ def test_labels_are_child_playouts(engine):
         reps = np.array([P // kk + (1 if m < P % kk else 0) for m in range(kk)], np.uint32)
         out = engine.playouts(np.array(children), reps, seed=seed, stream_base=base + i * P)
         sign = -1.0 if boards[i, 3] & 1 else 1.0
-        off = np.concatenate([[0], np.cumsum(reps)])
+        off = np.concatenate([[0], np.cumsum(reps)]).astype(np.int64)
         for m in range(kk):
             s = int(out[off[m]:off[m + 1]].astype(np.int64).sum())
             assert qd[i, m] == np.float32(sign * s) / np.float32(reps[m])
