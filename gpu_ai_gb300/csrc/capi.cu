@@ -389,4 +389,39 @@ int gpuai_random_positions(gpuai_ctx *ctx, uint64_t seed, uint32_t n, uint32_t m
   return GPUAI_OK;
 }
 
+int gpuai_selfplay_positions(gpuai_ctx *ctx, uint64_t seed, uint32_t n, uint32_t min_plies, uint32_t max_plies,
+                             int32_t policy, gpuai_board *d_out, void *stream) {
+  if (!ctx) return fail(GPUAI_ERR_INVALID, "gpuai_selfplay_positions: ctx is NULL");
+  if (n == 0) return GPUAI_OK;
+  if (!d_out) return fail(GPUAI_ERR_INVALID, "gpuai_selfplay_positions: d_out is NULL");
+  if (policy < 0 || policy > 2) return fail(GPUAI_ERR_INVALID, "gpuai_selfplay_positions: unknown policy %d", policy);
+  if (min_plies > max_plies || max_plies - min_plies == 0xffffffffu)
+    return fail(GPUAI_ERR_INVALID, "gpuai_selfplay_positions: bad ply range");
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  int rc = set_device(ctx);
+  if (rc) return rc;
+  CK(ga::launch_random_positions(seed, n, min_plies, max_plies, reinterpret_cast<ga::Board *>(d_out),
+                                 static_cast<cudaStream_t>(stream), policy),
+     "self-play positions kernel launch");
+  return GPUAI_OK;
+}
+
+int gpuai_apply_move(const gpuai_board *board, const gpuai_move *move, gpuai_board *out) {
+  if (!board || !move || !out) return fail(GPUAI_ERR_INVALID, "gpuai_apply_move: NULL");
+  if (move->from >= 32 || move->to >= 32 || move->jumps > 12)
+    return fail(GPUAI_ERR_INVALID, "gpuai_apply_move: malformed move record");
+  uint32_t removed = 0;
+  for (int j = 0; j < move->jumps; j++) {
+    if (move->removed[j] >= 32) return fail(GPUAI_ERR_INVALID, "gpuai_apply_move: malformed move record");
+    removed |= 1u << move->removed[j];
+  }
+  const uint32_t mover = (board->meta & 1u) ? board->p2 : board->p1;
+  if (!((mover >> move->from) & 1u) || (((board->p1 | board->p2) >> move->to) & 1u && move->to != move->from))
+    return fail(GPUAI_ERR_INVALID, "gpuai_apply_move: move does not fit the board");
+  ga::Board b{board->p1, board->p2, board->kings, board->meta};
+  ga::apply_move(b, move->from, move->to, removed);
+  *out = gpuai_board{b.p1, b.p2, b.kings, b.meta};
+  return GPUAI_OK;
+}
+
 }  // extern "C"

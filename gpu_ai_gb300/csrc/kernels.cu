@@ -263,6 +263,9 @@ __global__ void genmoves_kernel(const Board *pos, uint32_t n, uint8_t *out, uint
 
 // ---- seeded positions (thread per position, stream tag 1)
 
+// Position p: U{min_plies..max_plies} plies of POLICY from the standard
+// start (random stream (seed, p, 1)), stopping early at a finished game.
+template <int POLICY>
 __global__ void random_positions_kernel(uint64_t seed, uint32_t n, uint32_t min_plies,
                                         uint32_t max_plies, Board *out) {
   const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
@@ -273,7 +276,7 @@ __global__ void random_positions_kernel(uint64_t seed, uint32_t n, uint32_t min_
   const uint32_t np = min_plies + mulhi_index(rs.next(), max_plies - min_plies + 1u);
   for (uint32_t q = 0; q < np; q++) {
     if (((b.meta >> 8) & 0xffu) >= (uint32_t)kDrawPlies) break;
-    if (ply_random(b, rs) <= 0) break;
+    if (ply<POLICY>(b, rs) <= 0) break;
   }
   uint4 *dst = reinterpret_cast<uint4 *>(out + p);
   *dst = make_uint4(b.p1, b.p2, b.kings, b.meta);
@@ -317,10 +320,12 @@ cudaError_t launch_genmoves(const Board *pos, uint32_t n, void *out, uint32_t ma
 }
 
 cudaError_t launch_random_positions(uint64_t seed, uint32_t n, uint32_t min_plies,
-                                    uint32_t max_plies, Board *out, cudaStream_t s) {
+                                    uint32_t max_plies, Board *out, cudaStream_t s, int policy) {
   const int block = 128;
-  random_positions_kernel<<<(n + block - 1) / block, block, 0, s>>>(seed, n, min_plies, max_plies,
-                                                                   out);
+  const uint32_t grid = (n + block - 1) / block;
+  if (policy == 1) random_positions_kernel<1><<<grid, block, 0, s>>>(seed, n, min_plies, max_plies, out);
+  else if (policy == 2) random_positions_kernel<2><<<grid, block, 0, s>>>(seed, n, min_plies, max_plies, out);
+  else random_positions_kernel<0><<<grid, block, 0, s>>>(seed, n, min_plies, max_plies, out);
   return cudaGetLastError();
 }
 

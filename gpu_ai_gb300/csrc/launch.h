@@ -46,8 +46,9 @@ cudaError_t playout_occupancy(int policy, int block, int *blocks_per_sm);
 cudaError_t launch_playouts(const PlayoutArgs &a, int policy, int block, int grid, cudaStream_t s);
 cudaError_t launch_genmoves(const Board *pos, uint32_t n, void *out, uint32_t max_moves,
                             uint8_t *counts, uint32_t *status, cudaStream_t s);
+// Positions after U{min_plies..max_plies} plies of `policy` from the start.
 cudaError_t launch_random_positions(uint64_t seed, uint32_t n, uint32_t min_plies,
-                                    uint32_t max_plies, Board *out, cudaStream_t s);
+                                    uint32_t max_plies, Board *out, cudaStream_t s, int policy = 0);
 
 // Sets the calling thread's gpuai_last_error() message; returns code.
 int record_error(int code, const char *msg);

@@ -108,6 +108,9 @@ def load_library(path: str = LIB_PATH):
                                          ctypes.c_float, _f32p]
     lib.gpuai_label_positions.argtypes = [vp, vp, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_uint64,
                                           ctypes.c_int32, vp, vp, vp, vp]
+    lib.gpuai_selfplay_positions.argtypes = [vp, ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
+                                             ctypes.c_int32, vp, vp]
+    lib.gpuai_apply_move.argtypes = [_u32p, _u8p, _u32p]
     lib.gpuai_searches_set_net.argtypes = [vp, vp, ctypes.c_float, ctypes.c_float]
     for name in header_symbols():
         if name not in ("gpuai_last_error", "gpuai_destroy", "gpuai_searches_destroy", "gpuai_net_destroy"):
@@ -119,6 +122,16 @@ def load_library(path: str = LIB_PATH):
 def _check(rc: int):
     if rc != OK:
         raise GpuAIError(rc, load_library().gpuai_last_error().decode())
+
+
+def apply_move(board, move) -> np.ndarray:
+    """Board after `move` (a 32-byte record of the board's move list)."""
+    b = np.ascontiguousarray(board, dtype=np.uint32).reshape(4)
+    m = np.ascontiguousarray(move, dtype=np.uint8).reshape(32)
+    out = np.zeros(4, np.uint32)
+    lib = load_library()
+    _check(lib.gpuai_apply_move(b.ctypes.data_as(_u32p), m.ctypes.data_as(_u8p), out.ctypes.data_as(_u32p)))
+    return out
 
 
 def _boards(pos) -> np.ndarray:
@@ -200,6 +213,11 @@ class Engine:
         out = np.zeros((n, 4), dtype=np.uint32)
         _check(self.lib.gpuai_random_positions(self.ctx, seed, n, min_plies, max_plies, out.ctypes.data_as(_u32p)))
         return out
+
+    def selfplay_positions(self, seed: int, n: int, min_plies: int, max_plies: int, policy: int, d_out: int,
+                           stream: Optional[int] = None):
+        """Enqueue n self-play positions of `policy` into device buffer d_out (n x 16 bytes)."""
+        _check(self.lib.gpuai_selfplay_positions(self.ctx, seed, n, min_plies, max_plies, policy, d_out, stream))
 
     def label_positions(self, d_pos: int, n: int, playouts_per_position: int, seed: int, stream_base: int,
                         policy: int, d_value: int, d_move_q: int, d_nmoves: int, stream: Optional[int] = None):

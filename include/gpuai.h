@@ -100,6 +100,19 @@ int gpuai_genmoves(gpuai_ctx *ctx, const gpuai_board *pos, uint32_t n, gpuai_mov
 int gpuai_random_positions(gpuai_ctx *ctx, uint64_t seed, uint32_t n, uint32_t min_plies,
                            uint32_t max_plies, gpuai_board *out);
 
+/* Device-side variant for training data: n positions into d_out (device),
+ * position i after U{min_plies..max_plies} plies of `policy` (GPUAI_POLICY_*)
+ * from the standard start, stopping early at a finished game; enqueued on
+ * `stream` (NULL = legacy default stream).  With GPUAI_POLICY_RANDOM the
+ * positions equal gpuai_random_positions' for the same seed. */
+int gpuai_selfplay_positions(gpuai_ctx *ctx, uint64_t seed, uint32_t n, uint32_t min_plies, uint32_t max_plies,
+                             int32_t policy, gpuai_board *d_out, void *stream);
+
+/* Host-side State::move (src/state.cu:57-92): the board after `move`, a
+ * record of the board's legal move list (gpuai_genmoves).  Needs no context
+ * or device. */
+int gpuai_apply_move(const gpuai_board *board, const gpuai_move *move, gpuai_board *out);
+
 /* Number of SMs, and the launch shape of the uniform-random playout kernel. */
 int gpuai_device_info(gpuai_ctx *ctx, int32_t *sms, int32_t *blocks_per_sm, int32_t *block_threads);
 

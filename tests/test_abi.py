@@ -81,3 +81,27 @@ def _fresh_load(path):
         return E.load_library(path)
     finally:
         E._lib = saved
+
+
+def test_apply_move_equals_the_oracle(lib_built):
+    """gpuai_apply_move (host, no device) against the oracle's State::move on
+    every legal move of seeded positions."""
+    import numpy as np
+
+    import oracle_lib as L
+    boards = L.random_positions(77, 1000, 0, 80)
+    moves, counts = L.genmoves(boards)
+    checked = 0
+    for i in range(len(boards)):
+        for m in range(int(counts[i])):
+            want = boards[i:i + 1].copy()
+            assert L.oracle().or_apply_packed_b16(L._ptr(want, L._u32p),
+                                                  L._ptr(np.ascontiguousarray(moves[i, m]), L._u8p)) == 0
+            got = E.apply_move(boards[i], moves[i, m])
+            assert np.array_equal(got, want[0]), (i, m)
+            checked += 1
+    assert checked > 2000
+    bad = np.zeros(32, np.uint8)
+    bad[0] = 40  # from square out of range
+    with pytest.raises(E.GpuAIError):
+        E.apply_move(boards[0], bad)
