@@ -28,7 +28,7 @@ def test_train_and_evaluate_small(engine):
     from gpu_ai_gb300 import learn
     data = learn.make_dataset(engine, 40_000, playouts=256, seed=3, chunk=16384)
     m = data["boards"].shape[0]
-    assert 30_000 < m <= 40_000
+    assert 20_000 < m <= 40_000  # finished games (about a quarter at up to 90 plies) are dropped
     assert float(data["value"].abs().max()) <= 1.0
     tr, te = learn.split(data, 4000)
     net = Net(0, max_batch=4096, seed=1)
