@@ -60,7 +60,7 @@ def measured_peaks():
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
             return json.load(f), "measured"
     except OSError:
-        return {"sm_max_mhz": 2070.0, "hbm_gbs": 6800.0}, "fallback"
+        return {"sm_max_mhz": 2070.0, "hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
 
 
 class ClockSampler:
@@ -370,23 +370,99 @@ def run_searches(args):
     print(json.dumps(line), flush=True)
 
 
+def quick_net(args):
+    """The network file given with --net, or one trained here on 1M self-play
+    positions with 1,024-playout labels (a few seconds)."""
+    from gpu_ai_gb300 import Engine, Net
+    from gpu_ai_gb300 import learn
+    net = Net(0, max_batch=8192, seed=1)
+    if args.net:
+        net.load(args.net)
+        return net
+    data = learn.make_dataset(Engine(0), 1_000_000, 1024, seed=1)
+    learn.train(net, data, epochs=3, batch=8192, lr=1e-3)
+    return net
+
+
 def run_serve(args):
     """Serving loop: Poisson arrivals of search requests on 10K seeded games
     (0-60 random plies), time budgets U(10, 200) ms, continuous batching;
-    random and reference-heuristic playouts side by side."""
+    random playouts, reference-heuristic playouts and learned searches
+    (network leaf values and priors, 2 random playouts per leaf) side by side."""
     from gpu_ai_gb300.serve import simulate
     from gpu_ai_gb300 import POLICY_RANDOM, POLICY_REF_HEURISTIC
     res = {}
+    q = args.leaves if args.leaves <= 256 else 64
     for name, pol in (("random", POLICY_RANDOM), ("ref_heuristic", POLICY_REF_HEURISTIC)):
         res[name] = simulate(rate=args.rate, n_requests=args.requests, n_games=10000, budget_ms=(10.0, 200.0),
-                             policy=pol, leaves_per_search=args.leaves if args.leaves <= 256 else 64,
-                             playouts_per_leaf=args.playouts_per_leaf)
+                             policy=pol, leaves_per_search=q, playouts_per_leaf=args.playouts_per_leaf)
+    net = quick_net(args)
+    res["learned"] = simulate(rate=args.rate, n_requests=args.requests, n_games=10000, budget_ms=(10.0, 200.0),
+                              policy=POLICY_RANDOM, leaves_per_search=q, playouts_per_leaf=2, net=net)
+    res["learned"]["network"] = args.net or "trained here: 1M positions x 1024 playouts, 3 epochs"
     line = {"metric": "serving: search requests with continuous batching", "unit": "ms",
             "value": res["random"]["latency_ms_p99"], "higher_is_better": False, "n_gpus": 1,
             "data": "synthetic (seeded games, Poisson arrivals)",
             "config": {"workload": f"{args.requests} requests at {args.rate} req/s, budgets U(10,200) ms",
                        "leaves_per_search_per_step": args.leaves, "playouts_per_leaf": args.playouts_per_leaf},
-            "random": res["random"], "ref_heuristic": res["ref_heuristic"]}
+            "random": res["random"], "ref_heuristic": res["ref_heuristic"], "learned": res["learned"]}
+    print(json.dumps(line), flush=True)
+
+
+# FLOPs per position of one training step (forward + backward GEMMs, padded
+# shapes): forward 2*(192*256 + 256*256 + 256*1024), backward dH2, dH1 and the
+# three weight gradients.
+TRAIN_FLOPS_PER_POSITION = 2 * (192 * 256 + 256 * 256 + 256 * 1024) + 2 * (1024 * 256 + 256 * 256) + \
+    2 * (1024 * 256 + 256 * 256 + 256 * 192)
+
+
+def run_learned(args):
+    """Learned part end to end: self-play positions labelled with GPU playouts,
+    training with the library's forward/backward/Adam kernels, value MAE on
+    held-out positions, and a learned-vs-plain MCTS match at equal ms/move."""
+    from gpu_ai_gb300 import Engine, Net
+    from gpu_ai_gb300 import learn
+    from gpu_ai_gb300.match import play_match
+    peaks, peak_kind = measured_peaks()
+    eng = Engine(0)
+    t0 = time.perf_counter()
+    data = learn.make_dataset(eng, args.positions, args.label_playouts, seed=1)
+    tr, te = learn.split(data, 50_000)
+    net = Net(0, max_batch=8192, seed=1)
+    res = learn.train(net, tr, epochs=args.epochs, batch=8192, lr=1e-3, log_every=500)
+    # steady-state training step time (tensor-core GEMMs plus the loss / row-sum / Adam kernels)
+    import torch
+    b, z, qv = tr["boards"][:8192].contiguous(), tr["value"][:8192].contiguous(), tr["q"][:8192].contiguous()
+    for _ in range(5):
+        net.train_step(b.data_ptr(), z.data_ptr(), qv.data_ptr(), 8192, 0.0)
+    net.params()
+    k = 50
+    ts = time.perf_counter()
+    for _ in range(k):
+        net.train_step(b.data_ptr(), z.data_ptr(), qv.data_ptr(), 8192, 0.0)
+    net.params()
+    step_s = (time.perf_counter() - ts) / k
+    tflops = TRAIN_FLOPS_PER_POSITION * 8192 / step_s / 1e12
+    ev = learn.evaluate(net, eng, te)
+    m = play_match(net, eng, n_games=args.match_games, ms_per_move=args.ms, seed=5, leaves=64, plain_ppl=8,
+                   learned_ppl=2, value_weight=0.5, c_puct=1.5)
+    line = {
+        "metric": "learned-proposal MCTS score vs plain GPU MCTS at equal ms/move",
+        "value": m["learned_score"], "unit": "score (win 1, draw 0.5)", "higher_is_better": True, "n_gpus": 1,
+        "dtype": "bf16 (fp32 accumulation)", "data": "synthetic (GPU self-play positions, GPU playout labels)",
+        "config": {"workload": f"{args.positions} self-play positions x {args.label_playouts} playouts, "
+                               f"{args.epochs} epochs, {args.match_games} games at {args.ms} ms/move",
+                   "network": "129-256-256-(1024 logits + tanh value)"},
+        "ci95_wilson": m["ci95_wilson"], "ci95_normal": m["ci95_normal"], "match": m,
+        "labels": {"positions_kept": int(data["boards"].shape[0]), "seconds": data["label_seconds"],
+                   "playouts_per_s": data["playouts"] / data["label_seconds"]},
+        "training": {"steps": res["steps"], "batch": res["batch"], "seconds": res["train_seconds"],
+                     "positions_per_s": res["positions_per_s"], "loss_first": res["history"][0],
+                     "loss_last": res["history"][-1], "step_ms": step_s * 1e3,
+                     "tensor_tflops": tflops, "tensor_frac_of_bf16_peak": tflops / peaks["bf16_tflops"],
+                     "peak": f"{peaks['bf16_tflops']} TFLOP/s bf16 ({peak_kind})"},
+        "eval": ev, "seconds": time.perf_counter() - t0,
+    }
     print(json.dumps(line), flush=True)
 
 
@@ -399,7 +475,13 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--block", type=int, default=0, help="threads per block of the playout kernel (0: default)")
     ap.add_argument("--blocks-per-sm", type=int, default=0, help="resident blocks per SM (0: as many as fit)")
-    ap.add_argument("--workload", choices=["playouts", "searches", "serve"], default="playouts")
+    ap.add_argument("--workload", choices=["playouts", "searches", "serve", "learned"], default="playouts")
+    ap.add_argument("--net", default="", help="serve workload: network file for the learned leg")
+    ap.add_argument("--positions", type=int, default=10_000_000, help="learned workload: self-play positions")
+    ap.add_argument("--label-playouts", type=int, default=4096, help="learned workload: playouts per label")
+    ap.add_argument("--epochs", type=float, default=3.0, help="learned workload: training epochs")
+    ap.add_argument("--match-games", type=int, default=400, help="learned workload: match games")
+    ap.add_argument("--ms", type=float, default=100.0, help="learned workload: milliseconds per move")
     ap.add_argument("--rate", type=float, default=1000.0, help="serve workload: requests per second")
     ap.add_argument("--requests", type=int, default=2000, help="serve workload: number of requests")
     ap.add_argument("--games", type=int, default=2048, help="searches workload: number of games")
@@ -414,6 +496,8 @@ def main():
         run_searches(args)
     elif args.workload == "serve":
         run_serve(args)
+    elif args.workload == "learned":
+        run_learned(args)
     else:
         run_ours(args)
 

@@ -13,6 +13,10 @@ Because each search is advanced by its own warp in a fixed order and uses its
 own random-stream range, a request with a playout budget gets the same tree,
 and the same result, whether it runs alone or among other requests.
 
+With a policy/value network attached, the same loop serves learned searches
+(network leaf values and move priors; the network's forward pass runs once per
+step on the leaves of all admitted requests together).
+
 ``simulate()`` drives the loop with Poisson arrivals and reports latency
 percentiles, playouts/s and peak device memory.
 """
@@ -28,6 +32,7 @@ import numpy as np
 from .engine import POLICY_RANDOM, Searches
 
 NODE_BYTES = 52  # device bytes per tree node (record, board, parent, move)
+LEARNED_NODE_BYTES = 64  # learned searches: 32 FP16 move priors per node
 
 
 @dataclass
@@ -55,13 +60,18 @@ class Request:
 class SearchServer:
     def __init__(self, max_searches: int = 4096, pool_nodes: Optional[int] = None, pool_fraction: float = 0.25,
                  leaves_per_search: int = 64, playouts_per_leaf: int = 8, policy: int = POLICY_RANDOM,
-                 seed: int = 0, use_graph: bool = True, steps_per_poll: int = 2):
+                 seed: int = 0, use_graph: bool = True, steps_per_poll: int = 2, net=None,
+                 value_weight: float = 0.5, c_puct: float = 1.5):
+        node_bytes = NODE_BYTES + (LEARNED_NODE_BYTES if net is not None else 0)
         if pool_nodes is None:  # admission by free device memory
             import torch
             free, _ = torch.cuda.mem_get_info()
-            pool_nodes = int(free * pool_fraction) // NODE_BYTES
+            pool_nodes = int(free * pool_fraction) // node_bytes
         self.pool_nodes = pool_nodes
+        self.node_bytes = node_bytes
         self.s = Searches(max_searches, pool_nodes, leaves_per_search, playouts_per_leaf, policy, seed)
+        if net is not None:  # learned searches: network leaf values and move priors
+            self.s.set_net(net, value_weight, c_puct)
         self.q = leaves_per_search
         self.ppl = playouts_per_leaf
         self.use_graph = use_graph
@@ -127,7 +137,8 @@ class SearchServer:
 
 def simulate(rate: float = 1000.0, n_requests: int = 2000, n_games: int = 10000, budget_ms=(10.0, 200.0),
              policy: int = POLICY_RANDOM, seed: int = 1, leaves_per_search: int = 64, playouts_per_leaf: int = 8,
-             node_capacity: int = 65536, server: Optional[SearchServer] = None) -> dict:
+             node_capacity: int = 65536, server: Optional[SearchServer] = None, net=None,
+             value_weight: float = 0.5, c_puct: float = 1.5) -> dict:
     """Poisson arrivals at `rate` req/s of requests on positions drawn from
     `n_games` seeded games (0-60 random plies), time budgets U(budget_ms)."""
     from .engine import Engine
@@ -137,7 +148,7 @@ def simulate(rate: float = 1000.0, n_requests: int = 2000, n_games: int = 10000,
     budgets = rng.uniform(budget_ms[0], budget_ms[1], n_requests)
     picks = rng.integers(0, n_games, n_requests)
     srv = server or SearchServer(leaves_per_search=leaves_per_search, playouts_per_leaf=playouts_per_leaf,
-                                 policy=policy, seed=seed)
+                                 policy=policy, seed=seed, net=net, value_weight=value_weight, c_puct=c_puct)
     srv.t0 = time.perf_counter()
     i = 0
     while i < n_requests or srv.queue or srv.active:
@@ -158,7 +169,7 @@ def simulate(rate: float = 1000.0, n_requests: int = 2000, n_games: int = 10000,
         "latency_ms_p50": float(np.percentile(lat, 50)), "latency_ms_p99": float(np.percentile(lat, 99)),
         "latency_ms_max": float(lat.max()), "playouts_per_s": playouts / elapsed,
         "mean_playouts_per_request": playouts / max(1, len(srv.done)),
-        "peak_tree_bytes": srv.peak_nodes_reserved * NODE_BYTES, "pool_bytes": srv.pool_nodes * NODE_BYTES,
+        "peak_tree_bytes": srv.peak_nodes_reserved * srv.node_bytes, "pool_bytes": srv.pool_nodes * srv.node_bytes,
         "steps": srv.steps,
     }
     if server is None:
