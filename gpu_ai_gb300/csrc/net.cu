@@ -5,12 +5,14 @@
 // only evaluation function there).
 //
 // Every matrix product is one kernel, gemm_kernel: C = A * B^T with A (M x K)
-// and B (N x K) BF16 and K-major in global memory.  A CTA of four warps
-// computes one 128 x BN tile (BN <= 256): warp 0 streams 64-wide K blocks of A
-// and B through a shared-memory ring with TMA (128-byte swizzle), warp 1 issues
-// tcgen05.mma (M = 128, N = BN, K = 16 per instruction, FP32 accumulators in
-// 256 TMEM columns), then all four warps read the accumulators back (warp w
-// owns TMEM lanes 32w..32w+31, i.e. tile rows) and apply a fused epilogue.
+// and B (N x K) BF16 and K-major in global memory.  A CTA of eight warps
+// computes one 128 x BN tile (BN = 64..256): warp 0 streams 64-wide K blocks of
+// A and B through a shared-memory ring with TMA (128-byte swizzle), warp 1
+// issues tcgen05.mma (M = 128, N = BN, K = 16 per instruction, FP32
+// accumulators in TMEM), then all eight warps read the accumulators back
+// (warp w owns TMEM lanes 32(w%4).. , i.e. 32 tile rows, and half of the
+// columns) and apply a fused epilogue.  The ring is sized so that two CTAs fit
+// on an SM: one CTA's epilogue overlaps the other's loads and MMAs.
 //
 // Training step on a batch of B rows (a multiple of 128; rows past n are zero):
 //   features      X (B x 192), X^T
@@ -100,7 +102,8 @@ struct Epi {
 
 struct GemmArgs {
   uint32_t m_rows;        // rows of A (multiple of 128)
-  uint32_t bn;            // tile width = MMA N (multiple of 16, <= 256)
+  uint32_t bn;            // tile width = MMA N (64, 128, 192 or 256)
+  uint32_t tmem_cols;     // TMEM columns allocated (power of two >= bn)
   uint32_t kb_per_split;  // 64-wide K blocks per CTA
   uint32_t stages;        // shared-memory ring depth
   const uint32_t *dev_rows;  // optional device row count: tiles past it do nothing
@@ -108,9 +111,12 @@ struct GemmArgs {
   Epi e;
 };
 
-constexpr uint32_t kBM = 128, kBK = 64, kTmemCols = 256, kMaxStages = 4;
-constexpr uint32_t kABytes = kBM * kBK * 2;  // one A stage: 16 KiB
+constexpr uint32_t kBM = 128, kBK = 64, kMaxStages = 4;
+constexpr uint32_t kThreads = 256;            // 8 warps: two per TMEM lane quadrant in the epilogue
+constexpr uint32_t kABytes = kBM * kBK * 2;   // one A stage: 16 KiB
 constexpr uint32_t kSmemLimit = 227u * 1024u;
+constexpr uint32_t kRingBudget = 100u * 1024u;  // ring size that leaves room for two CTAs per SM
+constexpr uint32_t kSmemExtra = 1024u + 128u + 1024u;  // alignment slack, barriers, value-head partials
 
 __device__ __forceinline__ uint32_t pack2(float a, float b) {
   __nv_bfloat162 h = __floats2bfloat162_rn(a, b);  // a in the low half
@@ -185,7 +191,7 @@ __device__ __forceinline__ void epilogue32(const Epi &e, float (&v)[32], uint32_
   }
 }
 
-__global__ void __launch_bounds__(128, 1)
+__global__ void __launch_bounds__(kThreads, 2)
     gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, const GemmArgs g) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023u) & ~(uintptr_t)1023u);
@@ -195,6 +201,7 @@ __global__ void __launch_bounds__(128, 1)
   uint64_t *accf = empty + nst;
   uint32_t *tslot = reinterpret_cast<uint32_t *>(accf + 1);
   uint32_t *s_err = tslot + 1;
+  float *vpart = reinterpret_cast<float *>(smem + nst * stage_bytes + 128u);  // [2][128] value-head partial sums
   const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
   const uint32_t row0 = blockIdx.x * kBM;
   uint32_t rows = g.m_rows;
@@ -214,7 +221,7 @@ __global__ void __launch_bounds__(128, 1)
     tc::tma_prefetch_map(&tmA);
     tc::tma_prefetch_map(&tmB);
   }
-  if (warp == 2) tc::tmem_alloc(tslot, kTmemCols);
+  if (warp == 2) tc::tmem_alloc(tslot, g.tmem_cols);
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
@@ -260,22 +267,27 @@ __global__ void __launch_bounds__(128, 1)
     __syncwarp();
   }
 
-  // epilogue: thread = tile row warp*32 + lane
+  // epilogue: warp w reads TMEM lane quadrant w % 4 (tile rows 32(w%4)..) and
+  // column half w / 4 of the tile
   if (!tc::mbar_wait(accf, 0)) atomicOr(s_err, 1u);
   __syncwarp();  // lanes leave the wait one by one; tcgen05.ld needs the whole warp
   tc::fence_after_sync();
-  const uint32_t row = row0 + warp * 32u + lane;
+  const uint32_t quad = warp & 3u, half = warp >> 2;
+  const uint32_t trow = quad * 32u + lane, row = row0 + trow;
   const bool row_ok = row < rows && *s_err == 0;
   float vsum = 0.0f;
-  for (uint32_t c = 0; c < bn; c += 32) {
+  const uint32_t c_lo = half * (bn / 2), c_hi = c_lo + bn / 2;
+  for (uint32_t c = c_lo; c < c_hi; c += 32) {
     float v[32];
-    tc::tmem_load32(tmem + ((warp * 32u) << 16) + c, v);  // warp-collective: every lane takes part
+    tc::tmem_load32(tmem + ((quad * 32u) << 16) + c, v);  // warp-collective: every lane takes part
     if (row_ok) epilogue32(g.e, v, row, blockIdx.y * bn + c, blockIdx.z, vsum);
   }
-  if (row_ok && (g.e.flags & kEpiVdot)) g.e.vdot_out[row] = vsum + g.e.vdot_b[0];
+  if (g.e.flags & kEpiVdot) vpart[half * kBM + trow] = vsum;
 
   tc::fence_before_sync();
   __syncthreads();
+  if ((g.e.flags & kEpiVdot) && half == 0 && row_ok)  // the row's two column halves, in order
+    g.e.vdot_out[row] = vpart[trow] + vpart[kBM + trow] + g.e.vdot_b[0];
   if (*s_err) {
     if (threadIdx.x == 0) {
       atomicOr(g.status, kStatusNetWait);
@@ -286,7 +298,7 @@ __global__ void __launch_bounds__(128, 1)
   }
   if (warp == 2) {
     tc::fence_after_sync();
-    tc::tmem_dealloc(tmem, kTmemCols);
+    tc::tmem_dealloc(tmem, g.tmem_cols);
   }
 }
 
@@ -330,79 +342,86 @@ __global__ void features_kernel(const gpuai_board *boards, uint32_t n, const uin
   }
 }
 
-// One thread per row: value and policy loss terms and their gradients.
+// One warp per row: value and policy loss terms and their gradients.  Lane m
+// holds move m of the reference move list; moves with the same (from, to)
+// share one logit (the lowest such lane speaks for the pair).
 __global__ void loss_kernel(const gpuai_board *boards, const float *z, const float *q, uint32_t n, uint32_t rows,
                             float tau, float vcoef, const float *logits, const float *vraw, bf16 *dZ3, bf16 *dZ3t,
                             uint32_t ldt, float *dv, float *rowloss) {
-  const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31u;
+  constexpr uint32_t kFull = 0xffffffffu;
   if (r >= rows) return;
   if (r >= n) {
-    dv[r] = 0.0f;
-    rowloss[2 * r] = rowloss[2 * r + 1] = 0.0f;
+    if (lane == 0) {
+      dv[r] = 0.0f;
+      rowloss[2 * r] = rowloss[2 * r + 1] = 0.0f;
+    }
     return;
   }
   const float inv_n = 1.0f / (float)n;
-  const float th = tanhf(vraw[r]);
-  const float e = th - z[r];
-  dv[r] = vcoef * 2.0f * e * (1.0f - th * th) * inv_n;
-  rowloss[2 * r + 1] = e * e;
-  float ce = 0.0f;
+  if (lane == 0) {
+    const float th = tanhf(vraw[r]);
+    const float e = th - z[r];
+    dv[r] = vcoef * 2.0f * e * (1.0f - th * th) * inv_n;
+    rowloss[2 * r + 1] = e * e;
+  }
   const uint4 bv = __ldg(reinterpret_cast<const uint4 *>(boards) + r);
   const Board b{bv.x, bv.y, bv.z, bv.w};
   Side sd;
   make_side(b, sd);
   const uint32_t J = jumpers(sd);
   const int k = count_moves(sd, J);
-  if (k >= 1 && k <= (int)kMaxMoves) {
-    uint16_t pair[kMaxMoves] = {};
-    int np = 0;
-    float tp[kMaxMoves];
-    const float *qr = q + (size_t)r * kMaxMoves;
-    float qmax = -3.0e38f;
-    for (int m = 0; m < k; m++) qmax = fmaxf(qmax, qr[m]);
-    float tsum = 0.0f;
-    for (int m = 0; m < k; m++) tsum += expf((qr[m] - qmax) / tau);
-    int m = 0;
+  float ce = 0.0f;
+  if (k >= 1 && k <= (int)kMaxMoves) {  // uniform over the warp
+    uint32_t pi = 0x10000u + lane;      // distinct placeholder for lanes without a move
+    uint32_t m = 0;
     for_each_move(sd, J, [&](int from, int to, uint32_t, int, uint32_t) {
-      const uint16_t pi = (uint16_t)(from * 32 + to);
-      const float t = expf((qr[m] - qmax) / tau) / tsum;
-      int u = 0;
-      while (u < np && pair[u] != pi) u++;
-      if (u == np) {
-        pair[np] = pi;
-        tp[np] = 0.0f;
-        np++;
-      }
-      tp[u] += t;
+      if (m == lane) pi = (uint32_t)(from * 32 + to);
       m++;
       return false;
     });
-    const float *lr = logits + (size_t)r * kOut;
-    float lmax = -3.0e38f;
-    for (int u = 0; u < np; u++) lmax = fmaxf(lmax, lr[pair[u]]);
-    float s = 0.0f;
-    for (int u = 0; u < np; u++) s += expf(lr[pair[u]] - lmax);
-    const float logz = lmax + logf(s);
-    for (int u = 0; u < np; u++) {
-      const float lp = lr[pair[u]] - logz;
-      ce -= tp[u] * lp;
-      const bf16 gq = __float2bfloat16_rn((expf(lp) - tp[u]) * inv_n);
-      dZ3[(size_t)r * kOut + pair[u]] = gq;
-      dZ3t[(size_t)pair[u] * ldt + r] = gq;
+    const bool act = lane < (uint32_t)k;
+    const float qm = act ? q[(size_t)r * kMaxMoves + lane] : -3.0e38f;
+    float qmax = qm;
+    for (int o = 16; o; o >>= 1) qmax = fmaxf(qmax, __shfl_xor_sync(kFull, qmax, o));
+    const float et = act ? expf((qm - qmax) / tau) : 0.0f;
+    float tsum = et;
+    for (int o = 16; o; o >>= 1) tsum += __shfl_xor_sync(kFull, tsum, o);
+    const float t = et / tsum;
+    const uint32_t grp = __match_any_sync(kFull, pi);
+    const bool leader = act && (uint32_t)(__ffs(grp) - 1) == lane;
+    float tp = 0.0f;  // target of this lane's pair: sum over the lanes sharing it, in lane order
+    for (int j = 0; j < 32; j++) {
+      const float tj = __shfl_sync(kFull, t, j);
+      if ((grp >> j) & 1u) tp += tj;
     }
+    const float lg = leader ? logits[(size_t)r * kOut + pi] : -3.0e38f;
+    float lmax = lg;
+    for (int o = 16; o; o >>= 1) lmax = fmaxf(lmax, __shfl_xor_sync(kFull, lmax, o));
+    float sum = leader ? expf(lg - lmax) : 0.0f;
+    for (int o = 16; o; o >>= 1) sum += __shfl_xor_sync(kFull, sum, o);
+    const float logz = lmax + logf(sum);
+    if (leader) {
+      const float lp = lg - logz;
+      ce = -tp * lp;
+      const bf16 gq = __float2bfloat16_rn((expf(lp) - tp) * inv_n);
+      dZ3[(size_t)r * kOut + pi] = gq;
+      dZ3t[(size_t)pi * ldt + r] = gq;
+    }
+    for (int o = 16; o; o >>= 1) ce += __shfl_xor_sync(kFull, ce, o);
   }
-  rowloss[2 * r] = ce;
+  if (lane == 0) rowloss[2 * r] = ce;
 }
 
 // out[row] = sum over the first ncols columns of M[row] (times vec[col] if
-// given); one warp per row, fixed order.
-__global__ void rowsum_kernel(const bf16 *M, uint32_t nrows, uint32_t ncols, uint32_t ld, const float *vec,
-                              float *out) {
-  const uint32_t row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31u;
-  if (row >= nrows) return;
+// given); one block of 256 threads per row, fixed order.
+__global__ void __launch_bounds__(256) rowsum_kernel(const bf16 *M, uint32_t ncols, uint32_t ld, const float *vec,
+                                                     float *out) {
+  __shared__ float red[256];
+  const uint32_t row = blockIdx.x, tid = threadIdx.x;
   const bf16 *p = M + (size_t)row * ld;
   float s = 0.0f;
-  for (uint32_t c = lane * 8u; c < ncols; c += 256u) {
+  for (uint32_t c = tid * 8u; c < ncols; c += 2048u) {
     const uint4 u = *reinterpret_cast<const uint4 *>(p + c);
     const uint32_t w[4] = {u.x, u.y, u.z, u.w};
 #pragma unroll
@@ -412,40 +431,42 @@ __global__ void rowsum_kernel(const bf16 *M, uint32_t nrows, uint32_t ncols, uin
       s += vec ? b * vec[c + 2 * t + 1] : b;
     }
   }
-  for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-  if (lane == 0) out[row] = s;
+  red[tid] = s;
+  __syncthreads();
+  for (uint32_t o = 128; o; o >>= 1) {
+    if (tid < o) red[tid] += red[tid + o];
+    __syncthreads();
+  }
+  if (tid == 0) out[row] = red[0];
 }
 
-// out[0] = sum of v[0..n) (one warp, fixed order).
-__global__ void vecsum_kernel(const float *v, uint32_t n, float *out) {
-  const uint32_t lane = threadIdx.x & 31u;
-  float s = 0.0f;
-  for (uint32_t i = lane; i < n; i += 32) s += v[i];
-  for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-  if (lane == 0) out[0] = s;
-}
-
-// loss2 = {mean policy cross entropy, mean squared value error} (one block of 256).
-__global__ void loss_reduce_kernel(const float *rowloss, uint32_t n, float *loss2) {
-  __shared__ float sp[256], sv[256];
-  float a = 0.0f, b = 0.0f;
+// One block of 256: loss2 = {mean policy cross entropy, mean squared value
+// error} over the n rows, and dbv = sum of dv over all rows (fixed order).
+__global__ void loss_reduce_kernel(const float *rowloss, const float *dv, uint32_t n, uint32_t rows, float *loss2,
+                                   float *dbv) {
+  __shared__ float sp[256], sv[256], sd[256];
+  float a = 0.0f, b = 0.0f, c = 0.0f;
   for (uint32_t i = threadIdx.x; i < n; i += 256) {
     a += rowloss[2 * i];
     b += rowloss[2 * i + 1];
   }
+  for (uint32_t i = threadIdx.x; i < rows; i += 256) c += dv[i];
   sp[threadIdx.x] = a;
   sv[threadIdx.x] = b;
+  sd[threadIdx.x] = c;
   __syncthreads();
   for (uint32_t o = 128; o; o >>= 1) {
     if (threadIdx.x < o) {
       sp[threadIdx.x] += sp[threadIdx.x + o];
       sv[threadIdx.x] += sv[threadIdx.x + o];
+      sd[threadIdx.x] += sd[threadIdx.x + o];
     }
     __syncthreads();
   }
   if (threadIdx.x == 0) {
     loss2[0] = n ? sp[0] / (float)n : 0.0f;
     loss2[1] = n ? sv[0] / (float)n : 0.0f;
+    dbv[0] = sd[0];
   }
 }
 
@@ -609,19 +630,24 @@ cudaError_t make_map(CUtensorMap *m, const void *base, uint64_t rows, uint64_t k
 cudaError_t gemm(const CUtensorMap &a, const CUtensorMap &b, uint32_t m_rows, uint32_t n_total, uint32_t bn,
                  uint32_t kb_total, uint32_t splits, const uint32_t *dev_rows, uint32_t *status, const Epi &e,
                  cudaStream_t s) {
-  if (m_rows % kBM || bn % 16 || bn == 0 || bn > kTmemCols || n_total % bn || splits == 0 || kb_total % splits)
+  if (m_rows % kBM || bn % 64 || bn == 0 || bn > 256 || n_total % bn || splits == 0 || kb_total % splits)
     return cudaErrorInvalidValue;
+  if ((e.flags & kEpiVdot) && n_total != bn) return cudaErrorInvalidValue;  // the value head needs whole rows
   GemmArgs g;
   g.m_rows = m_rows;
   g.bn = bn;
+  g.tmem_cols = bn <= 64 ? 64u : (bn <= 128 ? 128u : 256u);
   g.kb_per_split = kb_total / splits;
-  g.stages = g.kb_per_split < kMaxStages ? g.kb_per_split : kMaxStages;
+  const uint32_t stage_bytes = kABytes + bn * 128u;
+  uint32_t st = kRingBudget / stage_bytes;
+  st = st < 2 ? 2 : (st > kMaxStages ? kMaxStages : st);
+  g.stages = g.kb_per_split < st ? g.kb_per_split : st;
   g.dev_rows = dev_rows;
   g.status = status;
   g.e = e;
-  const uint32_t smem = g.stages * (kABytes + bn * 128u) + 1024u + 128u;
+  const uint32_t smem = g.stages * stage_bytes + kSmemExtra;
   if (smem > kSmemLimit) return cudaErrorInvalidValue;
-  gemm_kernel<<<dim3(m_rows / kBM, n_total / bn, splits), 128, smem, s>>>(a, b, g);
+  gemm_kernel<<<dim3(m_rows / kBM, n_total / bn, splits), kThreads, smem, s>>>(a, b, g);
   return cudaGetLastError();
 }
 
@@ -631,7 +657,10 @@ uint32_t pick_splits(uint32_t kb, uint32_t target) {
   return 1;
 }
 
-constexpr uint32_t kSplit3 = 16, kSplit2 = 32, kSplit1 = 32;
+constexpr uint32_t kSplit3 = 8, kSplit2 = 32, kSplit1 = 16;
+// N tile of each product (the B operand's tensor-map box height)
+constexpr uint32_t kBnF1 = 128, kBnF2 = 256 /* value head: whole rows */, kBnF3 = 256, kBnB1 = 128, kBnB3 = 128,
+                   kBnB2 = 128, kBnB4 = 128, kBnB5 = 64;
 
 template <class T>
 cudaError_t dalloc(std::vector<void *> &allocs, T **p, size_t n) {
@@ -679,7 +708,7 @@ cudaError_t forward_impl(const gpuai_net *net, Fwd &w, const gpuai_board *boards
   e1.ld_b = kH;
   e1.out_t = net->H1t;
   e1.ld_t = net->rows;
-  if ((e = gemm(w.mX, net->mW1, rows, kH, kH, kInPad / kBK, 1, dev_n, status, e1, s)) != cudaSuccess) return e;
+  if ((e = gemm(w.mX, net->mW1, rows, kH, kBnF1, kInPad / kBK, 1, dev_n, status, e1, s)) != cudaSuccess) return e;
   Epi e2 = e1;
   e2.flags |= kEpiVdot;
   e2.bias = P + oB2;
@@ -688,13 +717,13 @@ cudaError_t forward_impl(const gpuai_net *net, Fwd &w, const gpuai_board *boards
   e2.vdot_w = P + oWV;
   e2.vdot_b = P + oBV;
   e2.vdot_out = w.vraw;
-  if ((e = gemm(w.mH1, net->mW2, rows, kH, kH, kH / kBK, 1, dev_n, status, e2, s)) != cudaSuccess) return e;
+  if ((e = gemm(w.mH1, net->mW2, rows, kH, kBnF2, kH / kBK, 1, dev_n, status, e2, s)) != cudaSuccess) return e;
   Epi e3;
   e3.flags = kEpiBias | kEpiF32;
   e3.bias = P + oB3;
   e3.out_f32 = w.logits;
   e3.ld_f32 = kOut;
-  return gemm(w.mH2, net->mW3, rows, kOut, kH, kH / kBK, 1, dev_n, status, e3, s);
+  return gemm(w.mH2, net->mW3, rows, kOut, kBnF3, kH / kBK, 1, dev_n, status, e3, s);
 }
 
 // Forward + backward on rows [0, n) of the training workspace; gradients are
@@ -709,7 +738,7 @@ cudaError_t backward_impl(gpuai_net *net, const gpuai_board *boards, const float
   if ((e = cudaMemset2DAsync(net->dZ3t, (size_t)L * sizeof(bf16), 0, (size_t)B * sizeof(bf16), kOut, s)) !=
       cudaSuccess)
     return e;
-  loss_kernel<<<B / 128, 128, 0, s>>>(boards, z, q, n, B, tau, vcoef, net->fw.logits, net->fw.vraw, net->dZ3,
+  loss_kernel<<<B / 4, 128, 0, s>>>(boards, z, q, n, B, tau, vcoef, net->fw.logits, net->fw.vraw, net->dZ3,
                                       net->dZ3t, L, net->dv, net->rowloss);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   Epi b1;
@@ -722,7 +751,7 @@ cudaError_t backward_impl(gpuai_net *net, const gpuai_board *boards, const float
   b1.ld_b = kH;
   b1.out_t = net->dZ2t;
   b1.ld_t = L;
-  if ((e = gemm(net->mdZ3, net->mW3T, B, kH, kH, kOut / kBK, 1, nullptr, net->status, b1, s)) != cudaSuccess)
+  if ((e = gemm(net->mdZ3, net->mW3T, B, kH, kBnB1, kOut / kBK, 1, nullptr, net->status, b1, s)) != cudaSuccess)
     return e;
   Epi b3;
   b3.flags = kEpiMask | kEpiB16T;
@@ -730,7 +759,7 @@ cudaError_t backward_impl(gpuai_net *net, const gpuai_board *boards, const float
   b3.ld_mask = kH;
   b3.out_t = net->dZ1t;
   b3.ld_t = L;
-  if ((e = gemm(net->mdZ2, net->mW2T, B, kH, kH, kH / kBK, 1, nullptr, net->status, b3, s)) != cudaSuccess)
+  if ((e = gemm(net->mdZ2, net->mW2T, B, kH, kBnB3, kH / kBK, 1, nullptr, net->status, b3, s)) != cudaSuccess)
     return e;
   const uint32_t kb = B / kBK;
   splits[2] = pick_splits(kb, kSplit3);
@@ -741,29 +770,28 @@ cudaError_t backward_impl(gpuai_net *net, const gpuai_board *boards, const float
   b2.out_f32 = net->p3;
   b2.ld_f32 = kH;
   b2.partial_stride = (uint64_t)kOut * kH;
-  if ((e = gemm(net->mdZ3t, net->mH2t, kOut, kH, kH, kb, splits[2], nullptr, net->status, b2, s)) != cudaSuccess)
+  if ((e = gemm(net->mdZ3t, net->mH2t, kOut, kH, kBnB2, kb, splits[2], nullptr, net->status, b2, s)) != cudaSuccess)
     return e;
   Epi b4;
   b4.flags = kEpiPartial;
   b4.out_f32 = net->p2;
   b4.ld_f32 = kH;
   b4.partial_stride = (uint64_t)kH * kH;
-  if ((e = gemm(net->mdZ2t, net->mH1t, kH, kH, kH, kb, splits[1], nullptr, net->status, b4, s)) != cudaSuccess)
+  if ((e = gemm(net->mdZ2t, net->mH1t, kH, kH, kBnB4, kb, splits[1], nullptr, net->status, b4, s)) != cudaSuccess)
     return e;
   Epi b5;
   b5.flags = kEpiPartial;
   b5.out_f32 = net->p1;
   b5.ld_f32 = kInPad;
   b5.partial_stride = (uint64_t)kH * kInPad;
-  if ((e = gemm(net->mdZ1t, net->mXt, kH, kInPad, kInPad, kb, splits[0], nullptr, net->status, b5, s)) !=
+  if ((e = gemm(net->mdZ1t, net->mXt, kH, kInPad, kBnB5, kb, splits[0], nullptr, net->status, b5, s)) !=
       cudaSuccess)
     return e;
-  rowsum_kernel<<<kH / 4, 128, 0, s>>>(net->dZ1t, kH, B, L, nullptr, net->grad + oB1);
-  rowsum_kernel<<<kH / 4, 128, 0, s>>>(net->dZ2t, kH, B, L, nullptr, net->grad + oB2);
-  rowsum_kernel<<<kOut / 4, 128, 0, s>>>(net->dZ3t, kOut, B, L, nullptr, net->grad + oB3);
-  rowsum_kernel<<<kH / 4, 128, 0, s>>>(net->H2t, kH, B, L, net->dv, net->grad + oWV);
-  vecsum_kernel<<<1, 32, 0, s>>>(net->dv, B, net->grad + oBV);
-  loss_reduce_kernel<<<1, 256, 0, s>>>(net->rowloss, n, net->loss2);
+  rowsum_kernel<<<kH, 256, 0, s>>>(net->dZ1t, B, L, nullptr, net->grad + oB1);
+  rowsum_kernel<<<kH, 256, 0, s>>>(net->dZ2t, B, L, nullptr, net->grad + oB2);
+  rowsum_kernel<<<kOut, 256, 0, s>>>(net->dZ3t, B, L, nullptr, net->grad + oB3);
+  rowsum_kernel<<<kH, 256, 0, s>>>(net->H2t, B, L, net->dv, net->grad + oWV);
+  loss_reduce_kernel<<<1, 256, 0, s>>>(net->rowloss, net->dv, n, B, net->loss2, net->grad + oBV);
   return cudaGetLastError();
 }
 
@@ -914,14 +942,14 @@ int gpuai_net_create(int device, uint32_t max_batch, uint64_t init_seed, gpuai_n
   if (e == cudaSuccess) e = dalloc(A, &net->in_z, L);
   if (e == cudaSuccess) e = dalloc(A, &net->in_q, (size_t)L * kMaxMoves);
   if (e != cudaSuccess) return fail(cuda_err(e, "gpuai_net_create: allocation"));
-  e = make_map(&net->mW1, net->W1b, kH, kInPad, 256);
-  if (e == cudaSuccess) e = make_map(&net->mW2, net->W2b, kH, kH, 256);
-  if (e == cudaSuccess) e = make_map(&net->mW3, net->W3b, kOut, kH, 256);
-  if (e == cudaSuccess) e = make_map(&net->mW2T, net->W2T, kH, kH, 256);
-  if (e == cudaSuccess) e = make_map(&net->mW3T, net->W3T, kH, kOut, 256);
-  if (e == cudaSuccess) e = make_map(&net->mXt, net->Xt, kInPad, L, kInPad);
-  if (e == cudaSuccess) e = make_map(&net->mH1t, net->H1t, kH, L, 256);
-  if (e == cudaSuccess) e = make_map(&net->mH2t, net->H2t, kH, L, 256);
+  e = make_map(&net->mW1, net->W1b, kH, kInPad, kBnF1);
+  if (e == cudaSuccess) e = make_map(&net->mW2, net->W2b, kH, kH, kBnF2);
+  if (e == cudaSuccess) e = make_map(&net->mW3, net->W3b, kOut, kH, kBnF3);
+  if (e == cudaSuccess) e = make_map(&net->mW2T, net->W2T, kH, kH, kBnB3);
+  if (e == cudaSuccess) e = make_map(&net->mW3T, net->W3T, kH, kOut, kBnB1);
+  if (e == cudaSuccess) e = make_map(&net->mXt, net->Xt, kInPad, L, kBnB5);
+  if (e == cudaSuccess) e = make_map(&net->mH1t, net->H1t, kH, L, kBnB4);
+  if (e == cudaSuccess) e = make_map(&net->mH2t, net->H2t, kH, L, kBnB2);
   if (e == cudaSuccess) e = make_map(&net->mdZ3, net->dZ3, L, kOut, kBM);
   if (e == cudaSuccess) e = make_map(&net->mdZ3t, net->dZ3t, kOut, L, kBM);
   if (e == cudaSuccess) e = make_map(&net->mdZ2, net->dZ2, L, kH, kBM);

@@ -186,9 +186,9 @@ __device__ void expand_at(const Pool &p, int32_t n, int32_t base, int k) {
 // src/mcts.cpp:95-136): untried children share them equally; otherwise in
 // proportion to UCB1 weights rounded down; the remainder goes one each to the
 // heaviest children (first on ties).  Weights that sum to zero count as
-// equal.  Calls emit(child, slots) for children given slots, in child order.
-template <class Emit>
-__device__ void split_slots(const Pool &p, int32_t first, int k, uint32_t parent_visits, uint32_t T, Emit &&emit) {
+// equal.  Fills give[0..k) and returns the number of children given slots.
+__device__ int split_slots(const Pool &p, int32_t first, int k, uint32_t parent_visits, uint32_t T,
+                           uint32_t *give) {
   const float lnN = logf((float)(parent_visits > 0 ? parent_visits : 1u));
   float wsum = 0.0f;
   int untried = 0;
@@ -199,7 +199,6 @@ __device__ void split_slots(const Pool &p, int32_t first, int k, uint32_t parent
   }
   const bool equal = untried == 0 && !(wsum > 0.0f);
   uint32_t assigned = 0;
-  uint32_t give[kMaxChildren];
   float w[kMaxChildren];
   for (int c = 0; c < k; c++) {
     const uint4 ci = p.info[first + c];
@@ -222,8 +221,9 @@ __device__ void split_slots(const Pool &p, int32_t first, int k, uint32_t parent
     give[opt]++;
     assigned++;
   }
-  for (int c = 0; c < k; c++)
-    if (give[c]) emit(first + c, give[c]);
+  int kids = 0;
+  for (int c = 0; c < k; c++) kids += give[c] != 0;
+  return kids;
 }
 
 // Learned searches: splits T slots over the k children of node n one slot at
@@ -232,10 +232,10 @@ __device__ void split_slots(const Pool &p, int32_t first, int k, uint32_t parent
 // score for the player to move at n (an unvisited child: n's own Q minus
 // kFpuReduction), P its prior (uniform when n has more than kPriors moves or
 // has not been evaluated), N = n's visits and n the child's, in leaf slots.
-template <class Emit>
-__device__ void split_puct(const Pool &p, int32_t n, int32_t first, int k, uint32_t parent_visits,
-                           uint32_t parent_score2, uint32_t st, uint32_t T, float c_puct, Emit &&emit) {
-  float q[kMaxChildren], pr[kMaxChildren], nv[kMaxChildren];
+// Fills give[0..k) and returns the number of children given slots.
+__device__ int split_puct(const Pool &p, int32_t n, int32_t first, int k, uint32_t parent_visits,
+                          uint32_t parent_score2, uint32_t st, uint32_t T, float c_puct, uint32_t *give) {
+  float q[kMaxChildren], u[kMaxChildren], pr[kMaxChildren], nv[kMaxChildren];
   const bool priors = (st & kEvaluated) && k <= (int)kPriors;
   const float fpu = parent_visits ? fmaxf(0.0f, 1.0f - 0.5f * (float)parent_score2 / (float)parent_visits -
                                                     kFpuReduction)
@@ -243,27 +243,30 @@ __device__ void split_puct(const Pool &p, int32_t n, int32_t first, int k, uint3
   for (int c = 0; c < k; c++) {
     const uint4 ci = p.info[first + c];
     q[c] = ci.z ? 0.5f * (float)ci.w / (float)ci.z : fpu;
-    nv[c] = (float)(ci.z / kUnits);
-    pr[c] = priors ? __half2float(p.prior[(size_t)n * kPriors + c]) : 1.0f / (float)k;
+    nv[c] = 1.0f + (float)(ci.z / kUnits);
+    pr[c] = c_puct * (priors ? __half2float(p.prior[(size_t)n * kPriors + c]) : 1.0f / (float)k);
+    u[c] = pr[c] / nv[c];  // exploration term without the sqrt(N) factor
+    give[c] = 0;
   }
   const float N = (float)(parent_visits / kUnits);
-  uint32_t give[kMaxChildren];
-  for (int c = 0; c < k; c++) give[c] = 0;
   for (uint32_t t = 0; t < T; t++) {
-    const float sq = c_puct * sqrtf(N + (float)t + 1.0f);
+    const float sq = sqrtf(N + (float)t + 1.0f);
     int best = 0;
     float bs = -3.0e38f;
     for (int c = 0; c < k; c++) {
-      const float sc = q[c] + sq * pr[c] / (1.0f + nv[c] + (float)give[c]);
+      const float sc = fmaf(sq, u[c], q[c]);
       if (sc > bs) {
         bs = sc;
         best = c;
       }
     }
     give[best]++;
+    nv[best] += 1.0f;
+    u[best] = pr[best] / nv[best];
   }
-  for (int c = 0; c < k; c++)
-    if (give[c]) emit(first + c, give[c]);
+  int kids = 0;
+  for (int c = 0; c < k; c++) kids += give[c] != 0;
+  return kids;
 }
 
 // One warp per search.  The frontier holds (node, slots) pairs; each round
@@ -342,11 +345,12 @@ __global__ void __launch_bounds__(32 * kSelectWarps) select_kernel(Pool p, Table
         leaf = T;
       }
       node_next += (int32_t)fit_end;
+      uint32_t give[kMaxChildren];  // this lane's split, written to the next frontier in pass 2
       if (e < nf && !leaf) {
         if (LEARNED)
-          split_puct(p, n, first, k, visits, score2, st, T, lrn.c_puct, [&](int32_t, uint32_t) { kids++; });
+          kids = (uint32_t)split_puct(p, n, first, k, visits, score2, st, T, lrn.c_puct, give);
         else
-          split_slots(p, first, k, visits, T, [&](int32_t, uint32_t) { kids++; });
+          kids = (uint32_t)split_slots(p, first, k, visits, T, give);
       }
       __syncwarp();
       // warp prefix sums of children entries and leaf slots
@@ -373,13 +377,12 @@ __global__ void __launch_bounds__(32 * kSelectWarps) select_kernel(Pool p, Table
           }
         } else {
           uint32_t w = kid_at;
-          auto put = [&](int32_t child, uint32_t cnt) {
-            f_node[wi][cur ^ 1][w] = child;
-            f_cnt[wi][cur ^ 1][w] = cnt;
-            w++;
-          };
-          if (LEARNED) split_puct(p, n, first, k, visits, score2, st, T, lrn.c_puct, put);
-          else split_slots(p, first, k, visits, T, put);
+          for (int c = 0; c < k; c++)
+            if (give[c]) {
+              f_node[wi][cur ^ 1][w] = first + c;
+              f_cnt[wi][cur ^ 1][w] = give[c];
+              w++;
+            }
         }
       }
       __syncwarp();
