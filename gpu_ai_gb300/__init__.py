@@ -9,6 +9,8 @@ from .engine import (  # noqa: F401
     ERR_LIMIT,
     ERR_NO_DEVICE,
     ERR_OOM,
+    LAYOUT_THREAD,
+    LAYOUT_WARP,
     OK,
     POLICY_EPS_GREEDY,
     POLICY_RANDOM,
@@ -33,4 +35,6 @@ __all__ = [
     "POLICY_RANDOM",
     "POLICY_REF_HEURISTIC",
     "POLICY_EPS_GREEDY",
+    "LAYOUT_THREAD",
+    "LAYOUT_WARP",
 ]

@@ -1,11 +1,13 @@
 """Autotuner for the playout kernel and the batched-search step.
 
-Sweeps, on the current GPU, (1) the playout kernel's launch shape (threads
-per block 64-512 x resident blocks per SM) on a batch of random playouts and
+Sweeps, on the current GPU, (1) the playout kernel's layout (a thread per
+playout, or a warp per playout with one lane per square) x launch shape
+(threads per block 64-512 x resident blocks per SM) on a batch of random
+playouts and
 (2) the batched-search step's leaves per search and playouts per leaf, and
 caches the fastest settings in a JSON file keyed by GPU name (default
 ``~/.cache/gpu_ai_gb300/autotune.json``).  ``apply(engine)`` sets a cached
-launch shape on an Engine.
+layout and launch shape on an Engine.
 
     python -m gpu_ai_gb300.autotune [--quick] [--cache PATH]
 """
@@ -18,7 +20,7 @@ import time
 
 import numpy as np
 
-from .engine import Engine, Searches
+from .engine import LAYOUT_THREAD, LAYOUT_WARP, Engine, Searches
 
 DEFAULT_CACHE = os.path.join(os.path.expanduser("~"), ".cache", "gpu_ai_gb300", "autotune.json")
 
@@ -38,21 +40,30 @@ def _time_playouts(eng: Engine, pos, reps, repeats: int) -> float:
     return best
 
 
-def tune_playouts(eng: Engine, n_pos=64, reps_per_pos=4096, repeats=3, blocks=(64, 128, 256, 512)):
+def tune_playouts(eng: Engine, n_pos=64, reps_per_pos=4096, repeats=3, blocks=(64, 128, 256, 512),
+                  layouts=(LAYOUT_THREAD, LAYOUT_WARP)):
     pos = eng.random_positions(2016, n_pos, 0, 30)
     reps = np.full(n_pos, reps_per_pos, np.uint32)
     total = n_pos * reps_per_pos
     results = []
-    for block in blocks:
-        eng.set_launch(0, block, 0)
-        mx = eng.get_launch(0)["max_blocks_per_sm"]
-        for per_sm in sorted({max(1, mx // 2), max(1, (3 * mx) // 4), mx}):
-            eng.set_launch(0, block, per_sm)
-            t = _time_playouts(eng, pos, reps, repeats)
-            results.append({"block_threads": block, "blocks_per_sm": per_sm, "seconds": t, "playouts_per_s": total / t})
+    for layout in layouts:
+        eng.set_layout(0, layout)
+        for block in blocks:
+            eng.set_launch(0, block, 0)
+            mx = eng.get_launch(0)["max_blocks_per_sm"]
+            for per_sm in sorted({max(1, mx // 2), max(1, (3 * mx) // 4), mx}):
+                eng.set_launch(0, block, per_sm)
+                t = _time_playouts(eng, pos, reps, repeats)
+                results.append({"layout": "warp" if layout == LAYOUT_WARP else "thread", "block_threads": block,
+                                "blocks_per_sm": per_sm, "seconds": t, "playouts_per_s": total / t})
     best = max(results, key=lambda r: r["playouts_per_s"])
-    eng.set_launch(0, best["block_threads"], best["blocks_per_sm"])
+    _set(eng, best)
     return best, results
+
+
+def _set(eng: Engine, p: dict):
+    eng.set_layout(0, LAYOUT_WARP if p.get("layout") == "warp" else LAYOUT_THREAD)
+    eng.set_launch(0, p["block_threads"], p["blocks_per_sm"])
 
 
 def tune_searches(n_games=512, leaves=(32, 64, 128, 256), ppls=(2, 4, 8), seed=7):
@@ -95,8 +106,7 @@ def apply(eng: Engine, cache: str = DEFAULT_CACHE) -> bool:
     entry = load(cache).get(gpu_name())
     if not entry:
         return False
-    p = entry["playouts"]
-    eng.set_launch(0, p["block_threads"], p["blocks_per_sm"])
+    _set(eng, entry["playouts"])
     return True
 
 

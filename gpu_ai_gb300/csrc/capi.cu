@@ -105,6 +105,7 @@ struct gpuai_ctx {
   int block[3] = {ga::kPlayoutBlock, ga::kPlayoutBlock, ga::kPlayoutBlock};
   int blocks_per_sm[3] = {0, 0, 0};  // resident blocks per SM used for the grid
   int max_blocks_per_sm[3] = {0, 0, 0};
+  int layout[3] = {ga::kLayoutThread, ga::kLayoutThread, ga::kLayoutThread};
   Control *ctl = nullptr;  // device
   DevBuf d_in, d_off, d_out, d_aux;
   HostBuf h_in, h_out;
@@ -130,7 +131,8 @@ int set_device(gpuai_ctx *ctx) {
 
 int grid_for(gpuai_ctx *ctx, int policy, uint32_t total) {
   long long resident = (long long)ctx->sms * ctx->blocks_per_sm[policy];
-  long long need = ((long long)total + ctx->block[policy] - 1) / ctx->block[policy];
+  const long long per_block = ctx->layout[policy] == ga::kLayoutWarp ? ctx->block[policy] / 32 : ctx->block[policy];
+  long long need = ((long long)total + per_block - 1) / per_block;
   long long g = need < resident ? need : resident;
   return (int)(g < 1 ? 1 : g);
 }
@@ -152,7 +154,8 @@ int launch_device(gpuai_ctx *ctx, const gpuai_board *d_pos, const uint32_t *d_of
   a.counter = &ctx->ctl->counter;
   a.status = &ctx->ctl->status;
   a.plies = &ctx->ctl->plies;
-  CK(ga::launch_playouts(a, policy, ctx->block[policy], grid_for(ctx, policy, total), s), "playout kernel launch");
+  CK(ga::launch_playouts(a, policy, ctx->block[policy], grid_for(ctx, policy, total), s, ctx->layout[policy]),
+     "playout kernel launch");
   return GPUAI_OK;
 }
 
@@ -236,12 +239,38 @@ int gpuai_set_launch(gpuai_ctx *ctx, int32_t policy, int32_t block_threads, int3
   int rc = set_device(ctx);
   if (rc) return rc;
   int maxb = 0;
-  CK(ga::playout_occupancy(policy, block_threads, &maxb), "occupancy query");
+  CK(ga::playout_occupancy(policy, block_threads, &maxb, ctx->layout[policy]), "occupancy query");
   if (maxb < 1) return fail(GPUAI_ERR_INVALID, "gpuai_set_launch: block of %d threads cannot be resident", block_threads);
   if (blocks_per_sm < 0) return fail(GPUAI_ERR_INVALID, "gpuai_set_launch: negative blocks_per_sm");
   ctx->block[policy] = block_threads;
   ctx->max_blocks_per_sm[policy] = maxb;
   ctx->blocks_per_sm[policy] = (blocks_per_sm == 0 || blocks_per_sm > maxb) ? maxb : blocks_per_sm;
+  return GPUAI_OK;
+}
+
+int gpuai_set_layout(gpuai_ctx *ctx, int32_t policy, int32_t layout) {
+  if (!ctx) return fail(GPUAI_ERR_INVALID, "gpuai_set_layout: ctx is NULL");
+  if (policy < 0 || policy > 2) return fail(GPUAI_ERR_INVALID, "gpuai_set_layout: unknown policy %d", policy);
+  if (layout != GPUAI_LAYOUT_THREAD && layout != GPUAI_LAYOUT_WARP)
+    return fail(GPUAI_ERR_INVALID, "gpuai_set_layout: unknown layout %d", layout);
+  if (layout == GPUAI_LAYOUT_WARP && policy != GPUAI_POLICY_RANDOM)
+    return fail(GPUAI_ERR_INVALID, "gpuai_set_layout: the warp layout plays the uniform random policy only");
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  int rc = set_device(ctx);
+  if (rc) return rc;
+  int maxb = 0;
+  CK(ga::playout_occupancy(policy, ctx->block[policy], &maxb, layout), "occupancy query");
+  if (maxb < 1) return fail(GPUAI_ERR_INVALID, "gpuai_set_layout: the kernel cannot be resident");
+  ctx->layout[policy] = layout;
+  ctx->max_blocks_per_sm[policy] = maxb;
+  ctx->blocks_per_sm[policy] = maxb;
+  return GPUAI_OK;
+}
+
+int gpuai_get_layout(gpuai_ctx *ctx, int32_t policy, int32_t *layout) {
+  if (!ctx || !layout) return fail(GPUAI_ERR_INVALID, "gpuai_get_layout: NULL");
+  if (policy < 0 || policy > 2) return fail(GPUAI_ERR_INVALID, "gpuai_get_layout: unknown policy %d", policy);
+  *layout = ctx->layout[policy];
   return GPUAI_OK;
 }
 

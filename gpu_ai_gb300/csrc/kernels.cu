@@ -233,6 +233,109 @@ __global__ void __launch_bounds__(BLOCK) playout_kernel(PlayoutArgs a) {
   }
 }
 
+// ---- warp per playout (uniform random policy)
+
+// Warp-cooperative layout, the shape of the reference's playoutKernel
+// (src/multiplePlayout.cu:14-52: one block of threads per playout, one thread
+// per square), kept as the alternative the autotuner measures against thread
+// per playout.  Lane s owns dark square s.  Each ply every lane counts the
+// legal moves that start on its square (only captures when the side to move
+// has one); a warp prefix sum over the lanes puts them in the reference's
+// move-list order (squares ascending, each square's moves in its DFS /
+// direction order).  Lane 0 draws the move index from the playout's stream
+// exactly as the thread-per-playout kernel does (one draw per ply with two or
+// more moves), the lane owning that index applies its move, and the board is
+// broadcast.  Outcomes equal the thread-per-playout kernel's bit for bit.
+template <int BLOCK>
+__global__ void __launch_bounds__(BLOCK) warp_playout_kernel(PlayoutArgs a) {
+  if (a.dev_sizes != nullptr) {
+    a.npos = __ldg(&a.dev_sizes[0]);
+    a.total = __ldg(&a.dev_sizes[1]);
+  }
+  const uint32_t lane = threadIdx.x & 31u;
+  const int sq = (int)lane;
+  unsigned long long plies_here = 0;
+  for (;;) {
+    uint32_t j = 0;
+    if (lane == 0) j = atomicAdd(a.counter, 1u);
+    j = __shfl_sync(kFull, j, 0);
+    if (j >= a.total) break;
+    const uint32_t p = position_of(a, j);
+    Board b = load_board(a.pos + p);
+    Stream rs;  // drawn by lane 0 only
+    rs.init(a.seed, stream_of(a, p, j), 0);
+    uint32_t game_plies = 0;
+    int outcome = 0;
+    for (;;) {
+      if (((b.meta >> 8) & 0xffu) >= (uint32_t)kDrawPlies) break;  // draw
+      Side s;
+      make_side(b, s);
+      const uint32_t J = jumpers(s);
+      uint32_t md[4];
+      direct_masks(s, md);
+      int cnt = 0;
+      if (J) {
+        if ((J >> sq) & 1u) cnt = capture_walk(s, sq, [](int, uint32_t, int, uint32_t) { return false; });
+      } else {
+        cnt = (int)(((md[0] >> sq) & 1u) + ((md[1] >> sq) & 1u) + ((md[2] >> sq) & 1u) + ((md[3] >> sq) & 1u));
+      }
+      if (__any_sync(kFull, cnt < 0)) {  // capture deeper than kMaxDepth
+        if (lane == 0) atomicOr(a.status, kStatusDepth);
+        outcome = 0;
+        break;
+      }
+      uint32_t incl = (uint32_t)cnt;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t t = __shfl_up_sync(kFull, incl, o);
+        if (lane >= (uint32_t)o) incl += t;
+      }
+      const uint32_t n = __shfl_sync(kFull, incl, 31);
+      if (n == 0) {
+        outcome = (b.meta & 1u) ? 1 : -1;  // side to move cannot move: loses
+        break;
+      }
+      uint32_t idx = 0;
+      if (lane == 0 && n >= 2) idx = mulhi_index(rs.next(), n);
+      idx = __shfl_sync(kFull, idx, 0);
+      const uint32_t excl = incl - (uint32_t)cnt;
+      const bool mine = idx >= excl && idx < incl;
+      const int owner = __ffs(__ballot_sync(kFull, mine)) - 1;
+      if (mine) {
+        uint32_t want = idx - excl;
+        if (J) {
+          capture_walk(s, sq, [&](int t, uint32_t removed, int, uint32_t) {
+            if (want-- != 0) return false;
+            apply_move(b, sq, t, removed);
+            return true;
+          });
+        } else {
+          for (int d = 0; d < 4; d++)
+            if ((md[d] >> sq) & 1u) {
+              if (want == 0) {
+                apply_move(b, sq, sq + step_off(sq, d), 0u);
+                break;
+              }
+              want--;
+            }
+        }
+      }
+      b.p1 = __shfl_sync(kFull, b.p1, owner);
+      b.p2 = __shfl_sync(kFull, b.p2, owner);
+      b.kings = __shfl_sync(kFull, b.kings, owner);
+      b.meta = __shfl_sync(kFull, b.meta, owner);
+      if (++game_plies > kMaxPlies) {
+        if (lane == 0) atomicOr(a.status, kStatusPlyCap);
+        outcome = 0;
+        break;
+      }
+      plies_here++;
+    }
+    if (lane == 0) a.out[j] = (int8_t)outcome;
+  }
+  if (a.plies != nullptr && lane == 0) atomicAdd(a.plies, plies_here);
+}
+
 // ---- move lists (thread per board)
 
 __global__ void genmoves_kernel(const Board *pos, uint32_t n, uint8_t *out, uint32_t max_moves,
@@ -294,7 +397,17 @@ static const void *kernel_for(int block) {
   }
 }
 
-static const void *playout_fn(int policy, int block) {
+static const void *warp_kernel_for(int block) {
+  switch (block) {
+    case 64: return (const void *)warp_playout_kernel<64>;
+    case 128: return (const void *)warp_playout_kernel<128>;
+    case 512: return (const void *)warp_playout_kernel<512>;
+    default: return (const void *)warp_playout_kernel<256>;
+  }
+}
+
+static const void *playout_fn(int policy, int block, int layout) {
+  if (layout == kLayoutWarp) return warp_kernel_for(block);
   if (policy == 1) return kernel_for<1>(block);
   if (policy == 2) return kernel_for<2>(block);
   return kernel_for<0>(block);
@@ -302,13 +415,14 @@ static const void *playout_fn(int policy, int block) {
 
 bool valid_block(int block) { return block == 64 || block == 128 || block == 256 || block == 512; }
 
-cudaError_t playout_occupancy(int policy, int block, int *blocks_per_sm) {
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, playout_fn(policy, block), block, 0);
+cudaError_t playout_occupancy(int policy, int block, int *blocks_per_sm, int layout) {
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, playout_fn(policy, block, layout), block, 0);
 }
 
-cudaError_t launch_playouts(const PlayoutArgs &a, int policy, int block, int grid, cudaStream_t s) {
+cudaError_t launch_playouts(const PlayoutArgs &a, int policy, int block, int grid, cudaStream_t s, int layout) {
+  if (layout == kLayoutWarp && policy != 0) return cudaErrorInvalidValue;
   void *args[] = {const_cast<PlayoutArgs *>(&a)};
-  return cudaLaunchKernel(playout_fn(policy, block), dim3(grid), dim3(block), args, 0, s);
+  return cudaLaunchKernel(playout_fn(policy, block, layout), dim3(grid), dim3(block), args, 0, s);
 }
 
 cudaError_t launch_genmoves(const Board *pos, uint32_t n, void *out, uint32_t max_moves,

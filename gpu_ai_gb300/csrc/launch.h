@@ -39,11 +39,16 @@ struct PlayoutArgs {
   const uint32_t *dev_sizes = nullptr;
 };
 
+// Playout layouts: a thread per playout (every policy) or a warp per playout
+// (uniform random policy only; same outcomes).
+constexpr int kLayoutThread = 0, kLayoutWarp = 1;
+
 // Playout kernels are instantiated for blocks of 64, 128, 256 and 512 threads.
 bool valid_block(int block);
 // Resident blocks per SM of the playout kernel for `policy` and `block`.
-cudaError_t playout_occupancy(int policy, int block, int *blocks_per_sm);
-cudaError_t launch_playouts(const PlayoutArgs &a, int policy, int block, int grid, cudaStream_t s);
+cudaError_t playout_occupancy(int policy, int block, int *blocks_per_sm, int layout = kLayoutThread);
+cudaError_t launch_playouts(const PlayoutArgs &a, int policy, int block, int grid, cudaStream_t s,
+                            int layout = kLayoutThread);
 cudaError_t launch_genmoves(const Board *pos, uint32_t n, void *out, uint32_t max_moves,
                             uint8_t *counts, uint32_t *status, cudaStream_t s);
 // Positions after U{min_plies..max_plies} plies of `policy` from the start.

@@ -25,6 +25,9 @@ POLICY_RANDOM = 0
 POLICY_REF_HEURISTIC = 1
 POLICY_EPS_GREEDY = 2
 
+LAYOUT_THREAD = 0
+LAYOUT_WARP = 1
+
 OK = 0
 ERR_INVALID = -1
 ERR_CUDA = -2
@@ -111,6 +114,8 @@ def load_library(path: str = LIB_PATH):
     lib.gpuai_selfplay_positions.argtypes = [vp, ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
                                              ctypes.c_int32, vp, vp]
     lib.gpuai_apply_move.argtypes = [_u32p, _u8p, _u32p]
+    lib.gpuai_set_layout.argtypes = [vp, ctypes.c_int32, ctypes.c_int32]
+    lib.gpuai_get_layout.argtypes = [vp, ctypes.c_int32, _i32p]
     lib.gpuai_searches_set_net.argtypes = [vp, vp, ctypes.c_float, ctypes.c_float]
     for name in header_symbols():
         if name not in ("gpuai_last_error", "gpuai_destroy", "gpuai_searches_destroy", "gpuai_net_destroy"):
@@ -227,6 +232,15 @@ class Engine:
 
     def set_launch(self, policy: int, block_threads: int, blocks_per_sm: int = 0):
         _check(self.lib.gpuai_set_launch(self.ctx, policy, block_threads, blocks_per_sm))
+
+    def set_layout(self, policy: int, layout: int):
+        """LAYOUT_THREAD (thread per playout) or LAYOUT_WARP (warp per playout, random policy)."""
+        _check(self.lib.gpuai_set_layout(self.ctx, policy, layout))
+
+    def get_layout(self, policy: int = POLICY_RANDOM) -> int:
+        v = ctypes.c_int32()
+        _check(self.lib.gpuai_get_layout(self.ctx, policy, ctypes.byref(v)))
+        return v.value
 
     def get_launch(self, policy: int = POLICY_RANDOM):
         a, b, c = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()

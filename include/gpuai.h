@@ -127,6 +127,17 @@ int gpuai_set_launch(gpuai_ctx *ctx, int32_t policy, int32_t block_threads, int3
 int gpuai_get_launch(gpuai_ctx *ctx, int32_t policy, int32_t *block_threads, int32_t *blocks_per_sm,
                      int32_t *max_blocks_per_sm);
 
+/* Playout layout for `policy`: a thread per playout (GPUAI_LAYOUT_THREAD, the
+ * default, every policy) or a warp per playout with one lane per dark square
+ * (GPUAI_LAYOUT_WARP, uniform random policy only), the shape of the
+ * reference's playoutKernel (src/multiplePlayout.cu:14-52).  Outcomes are the
+ * same in both layouts; the autotuner measures which is faster.  Setting a
+ * layout resets blocks_per_sm to as many as fit. */
+#define GPUAI_LAYOUT_THREAD 0
+#define GPUAI_LAYOUT_WARP 1
+int gpuai_set_layout(gpuai_ctx *ctx, int32_t policy, int32_t layout);
+int gpuai_get_layout(gpuai_ctx *ctx, int32_t policy, int32_t *layout);
+
 /* ---- many searches with device-resident trees ----
  * Replaces the reference's one-search-per-MCTSPlayer loop
  * (src/player.cpp:134-150, src/mcts.cpp:63-191) with searches whose UCT trees
