@@ -416,6 +416,81 @@ TRAIN_FLOPS_PER_POSITION = 2 * (192 * 256 + 256 * 256 + 256 * 1024) + 2 * (1024 
     2 * (1024 * 256 + 256 * 256 + 256 * 192)
 
 
+def _train_rows(n, seed=3):
+    """n seeded positions (0-60 random plies, 1-32 legal moves) with random
+    value and move-value targets, as device tensors."""
+    import torch
+    from gpu_ai_gb300 import Engine
+    eng = Engine(0)
+    pos = eng.random_positions(seed, 3 * n, 0, 60)
+    _, counts = eng.genmoves(pos)
+    pos = pos[(counts > 0) & (counts <= 32)][:n]
+    rng = np.random.default_rng(seed)
+    b = torch.from_numpy(np.ascontiguousarray(pos).view(np.int32)).cuda()
+    z = torch.from_numpy(rng.uniform(-1, 1, n).astype(np.float32)).cuda()
+    q = torch.from_numpy(rng.uniform(-1, 1, (n, 32)).astype(np.float32)).cuda()
+    return b, z, q
+
+
+def run_train(args):
+    """Network training steps at batch 8192 (features, 8 tcgen05 GEMMs, loss,
+    bias sums, Adam): positions/s and tensor TFLOP/s against the measured BF16
+    peak.  Host-timed over K steps on the network's stream (synchronised on
+    both sides); inputs stay resident."""
+    from gpu_ai_gb300 import Net
+    peaks, peak_kind = measured_peaks()
+    n = 8192
+    b, z, q = _train_rows(n)
+    net = Net(0, max_batch=n, seed=1)
+    for _ in range(args.warmup):
+        net.train_step(b.data_ptr(), z.data_ptr(), q.data_ptr(), n, 1e-4)
+    net.params()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        net.train_step(b.data_ptr(), z.data_ptr(), q.data_ptr(), n, 1e-4)
+    net.params()
+    el = time.perf_counter() - t0
+    step_s = el / max(1, args.steps)
+    tflops = TRAIN_FLOPS_PER_POSITION * n / step_s / 1e12
+    print(json.dumps({
+        "metric": "policy/value network training throughput", "value": n / step_s, "unit": "positions/s",
+        "higher_is_better": True, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": step_s * 1e3, "dtype": "bf16 (fp32 accumulation)",
+        "data": "synthetic (seeded positions, random targets)",
+        "config": {"workload": "Adam steps on 8192 positions, 129-256-256-(1024+1)", "batch": n},
+        "roofline": {"bound": "tensor", "achieved": tflops, "peak": peaks["bf16_tflops"], "unit": "TFLOP/s",
+                     "frac": tflops / peaks["bf16_tflops"], "peak_kind": peak_kind,
+                     "flop_per_position": TRAIN_FLOPS_PER_POSITION},
+    }), flush=True)
+
+
+def run_learned_search(args):
+    """Learned device searches: 400 searches x 64 leaves per step, 2 playouts
+    per leaf, network forward on every leaf; K eager steps timed."""
+    from gpu_ai_gb300 import Engine, Net, Searches
+    eng = Engine(0)
+    net = Net(0, max_batch=256, seed=1)
+    roots = eng.random_positions(5, 400, 0, 60)
+    s = Searches(400, 400 * 20000, 64, 2, seed=1)
+    s.set_net(net, 0.5, 1.5)
+    for i, r in enumerate(roots):
+        s.add(r, 1 << 40, 20000, i << 40)
+    for _ in range(args.warmup):
+        s.step(1, 64, False)
+    s.poll()
+    t0 = time.perf_counter()
+    s.step(args.steps, 64, False)
+    done, _ = s.poll()
+    el = time.perf_counter() - t0
+    leaves = 400 * 64 * args.steps
+    print(json.dumps({
+        "metric": "learned search steps", "value": leaves / el, "unit": "leaf evaluations/s",
+        "higher_is_better": True, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": el / max(1, args.steps) * 1e3, "dtype": "bf16 network, u32 playouts",
+        "data": "synthetic (seeded positions)",
+        "config": {"workload": "400 searches x 64 leaves/step, 2 playouts/leaf, lambda 0.5"}}), flush=True)
+
+
 def run_learned(args):
     """Learned part end to end: self-play positions labelled with GPU playouts,
     training with the library's forward/backward/Adam kernels, value MAE on
@@ -475,7 +550,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--block", type=int, default=0, help="threads per block of the playout kernel (0: default)")
     ap.add_argument("--blocks-per-sm", type=int, default=0, help="resident blocks per SM (0: as many as fit)")
-    ap.add_argument("--workload", choices=["playouts", "searches", "serve", "learned"], default="playouts")
+    ap.add_argument("--workload", choices=["playouts", "searches", "serve", "learned", "train", "learned-search"],
+                    default="playouts")
     ap.add_argument("--net", default="", help="serve workload: network file for the learned leg")
     ap.add_argument("--positions", type=int, default=10_000_000, help="learned workload: self-play positions")
     ap.add_argument("--label-playouts", type=int, default=4096, help="learned workload: playouts per label")
@@ -498,6 +574,10 @@ def main():
         run_serve(args)
     elif args.workload == "learned":
         run_learned(args)
+    elif args.workload == "train":
+        run_train(args)
+    elif args.workload == "learned-search":
+        run_learned_search(args)
     else:
         run_ours(args)
 
