@@ -131,14 +131,28 @@ __device__ __forceinline__ bool positive_bf(uint32_t h16) { return (h16 & 0x8000
 __device__ __forceinline__ void epilogue32(const Epi &e, float (&v)[32], uint32_t row, uint32_t col0,
                                            uint32_t split, float &vsum) {
   const uint32_t f = e.flags;
-  if (f & kEpiBias) {
+  if (f & kEpiBias) {  // column vectors are 16-byte aligned: col0 is a multiple of 32
+    const float4 *bp = reinterpret_cast<const float4 *>(e.bias + col0);
 #pragma unroll
-    for (int j = 0; j < 32; j++) v[j] += __ldg(&e.bias[col0 + j]);
+    for (int q = 0; q < 8; q++) {
+      const float4 t = __ldg(bp + q);
+      v[4 * q] += t.x;
+      v[4 * q + 1] += t.y;
+      v[4 * q + 2] += t.z;
+      v[4 * q + 3] += t.w;
+    }
   }
   if (f & kEpiRank1) {
     const float r = e.r1_row[row];
+    const float4 *cp = reinterpret_cast<const float4 *>(e.r1_col + col0);
 #pragma unroll
-    for (int j = 0; j < 32; j++) v[j] = fmaf(r, __ldg(&e.r1_col[col0 + j]), v[j]);
+    for (int q = 0; q < 8; q++) {
+      const float4 t = __ldg(cp + q);
+      v[4 * q] = fmaf(r, t.x, v[4 * q]);
+      v[4 * q + 1] = fmaf(r, t.y, v[4 * q + 1]);
+      v[4 * q + 2] = fmaf(r, t.z, v[4 * q + 2]);
+      v[4 * q + 3] = fmaf(r, t.w, v[4 * q + 3]);
+    }
   }
   if (f & kEpiRelu) {
 #pragma unroll
@@ -182,10 +196,14 @@ __device__ __forceinline__ void epilogue32(const Epi &e, float (&v)[32], uint32_
       }
     }
     if (f & kEpiVdot) {
+      const float4 *wp = reinterpret_cast<const float4 *>(e.vdot_w + col0);
 #pragma unroll
-      for (int t = 0; t < 16; t++) {
-        vsum = fmaf(lo_bf(p[t]), __ldg(&e.vdot_w[col0 + 2 * t]), vsum);
-        vsum = fmaf(hi_bf(p[t]), __ldg(&e.vdot_w[col0 + 2 * t + 1]), vsum);
+      for (int q = 0; q < 8; q++) {
+        const float4 t = __ldg(wp + q);
+        vsum = fmaf(lo_bf(p[2 * q]), t.x, vsum);
+        vsum = fmaf(hi_bf(p[2 * q]), t.y, vsum);
+        vsum = fmaf(lo_bf(p[2 * q + 1]), t.z, vsum);
+        vsum = fmaf(hi_bf(p[2 * q + 1]), t.w, vsum);
       }
     }
   }
@@ -677,12 +695,13 @@ uint32_t round128(uint32_t n) { return (n + 127u) / 128u * 128u; }
 
 }  // namespace
 
-cudaError_t fwd_alloc(Fwd &w, uint32_t rows, std::vector<void *> &allocs) {
+cudaError_t fwd_alloc(Fwd &w, uint32_t rows, std::vector<void *> &allocs, bool bf16_logits) {
   w.rows = round128(rows ? rows : 1);
   cudaError_t e = dalloc(allocs, &w.X, (size_t)w.rows * kInPad);
   if (e == cudaSuccess) e = dalloc(allocs, &w.H1, (size_t)w.rows * kH);
   if (e == cudaSuccess) e = dalloc(allocs, &w.H2, (size_t)w.rows * kH);
-  if (e == cudaSuccess) e = dalloc(allocs, &w.logits, (size_t)w.rows * kOut);
+  if (e == cudaSuccess && bf16_logits) e = dalloc(allocs, &w.logits_b, (size_t)w.rows * kOut);
+  if (e == cudaSuccess && !bf16_logits) e = dalloc(allocs, &w.logits, (size_t)w.rows * kOut);
   if (e == cudaSuccess) e = dalloc(allocs, &w.vraw, (size_t)w.rows);
   if (e == cudaSuccess) e = make_map(&w.mX, w.X, w.rows, kInPad, kBM);
   if (e == cudaSuccess) e = make_map(&w.mH1, w.H1, w.rows, kH, kBM);
@@ -719,10 +738,12 @@ cudaError_t forward_impl(const gpuai_net *net, Fwd &w, const gpuai_board *boards
   e2.vdot_out = w.vraw;
   if ((e = gemm(w.mH1, net->mW2, rows, kH, kBnF2, kH / kBK, 1, dev_n, status, e2, s)) != cudaSuccess) return e;
   Epi e3;
-  e3.flags = kEpiBias | kEpiF32;
+  e3.flags = kEpiBias | (w.logits_b ? kEpiB16 : kEpiF32);
   e3.bias = P + oB3;
   e3.out_f32 = w.logits;
   e3.ld_f32 = kOut;
+  e3.out_b = w.logits_b;
+  e3.ld_b = kOut;
   return gemm(w.mH2, net->mW3, rows, kOut, kBnF3, kH / kBK, 1, dev_n, status, e3, s);
 }
 
@@ -921,7 +942,7 @@ int gpuai_net_create(int device, uint32_t max_batch, uint64_t init_seed, gpuai_n
   if (e == cudaSuccess) e = dalloc(A, &net->W3b, (size_t)kOut * kH);
   if (e == cudaSuccess) e = dalloc(A, &net->W2T, (size_t)kH * kH);
   if (e == cudaSuccess) e = dalloc(A, &net->W3T, (size_t)kH * kOut);
-  if (e == cudaSuccess) e = fwd_alloc(net->fw, L, A);
+  if (e == cudaSuccess) e = fwd_alloc(net->fw, L, A, false);
   if (e == cudaSuccess) e = dalloc(A, &net->Xt, (size_t)kInPad * L);
   if (e == cudaSuccess) e = dalloc(A, &net->H1t, (size_t)kH * L);
   if (e == cudaSuccess) e = dalloc(A, &net->H2t, (size_t)kH * L);

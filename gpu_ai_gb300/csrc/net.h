@@ -39,17 +39,19 @@ constexpr uint32_t kStatusNetWait = 16u;  // a tensor-core kernel gave up waitin
 struct Fwd {
   uint32_t rows = 0;
   __nv_bfloat16 *X = nullptr, *H1 = nullptr, *H2 = nullptr;
-  float *logits = nullptr, *vraw = nullptr;
+  float *logits = nullptr, *vraw = nullptr;  // FP32 logits (training, host forward) ...
+  __nv_bfloat16 *logits_b = nullptr;         // ... or BF16 logits (search leaves: priors only)
   CUtensorMap mX, mH1, mH2;
 };
 
 // CUDA device the network lives on.
 int device_of(const gpuai_net *net);
 
-// Allocates a workspace (device allocations appended to `allocs`).
-cudaError_t fwd_alloc(Fwd &w, uint32_t rows, std::vector<void *> &allocs);
+// Allocates a workspace (device allocations appended to `allocs`); the logits
+// are stored in BF16 when bf16_logits is set, else in FP32.
+cudaError_t fwd_alloc(Fwd &w, uint32_t rows, std::vector<void *> &allocs, bool bf16_logits);
 
-// Features, three GEMMs: w.logits (rows x 1024, bias added) and w.vraw (the
+// Features, three GEMMs: w.logits or w.logits_b (rows x 1024, bias added) and w.vraw (the
 // value before tanh) for boards[0..n).  With dev_n set, n is read from device
 // memory (launches inside a CUDA graph); tiles past it do no work.
 cudaError_t forward(const gpuai_net *net, Fwd &w, const gpuai_board *boards, uint32_t n, const uint32_t *dev_n,

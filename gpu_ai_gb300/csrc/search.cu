@@ -454,7 +454,8 @@ __global__ void backprop_learned_kernel(Pool p, Table t, Leaves l, uint32_t ppl,
 // head, for the side to move) and, the first time a node is a leaf, its
 // moves' priors: the softmax of the move logits over its legal (from, to)
 // pairs, a pair's probability shared equally by the moves that have it.
-__global__ void leaf_eval_kernel(Pool p, Leaves l, const float *logits, const float *vraw, uint32_t max_leaves) {
+__global__ void leaf_eval_kernel(Pool p, Leaves l, const __nv_bfloat16 *logits, const float *vraw,
+                                 uint32_t max_leaves) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= max_leaves || i >= l.sizes[0]) return;
   l.value[i] = tanhf(vraw[i]);
@@ -485,14 +486,18 @@ __global__ void leaf_eval_kernel(Pool p, Leaves l, const float *logits, const fl
       of[m++] = (uint8_t)u;
       return false;
     });
-    const float *lr = logits + (size_t)i * net::kOut;
+    const __nv_bfloat16 *lr = logits + (size_t)i * net::kOut;
+    float lg[kPriors];
     float lmax = -3.0e38f;
-    for (int u = 0; u < np; u++) lmax = fmaxf(lmax, lr[pair[u]]);
+    for (int u = 0; u < np; u++) {
+      lg[u] = __bfloat162float(lr[pair[u]]);
+      lmax = fmaxf(lmax, lg[u]);
+    }
     float sum = 0.0f;
-    for (int u = 0; u < np; u++) sum += expf(lr[pair[u]] - lmax);
+    for (int u = 0; u < np; u++) sum += expf(lg[u] - lmax);
     for (int j = 0; j < k; j++) {
       const int u = of[j];
-      p.prior[(size_t)n * kPriors + j] = __float2half(expf(lr[pair[u]] - lmax) / sum / (float)mult[u]);
+      p.prior[(size_t)n * kPriors + j] = __float2half(expf(lg[u] - lmax) / sum / (float)mult[u]);
     }
   }
   atomicOr(&p.info[n].y, kEvaluated << 16);
@@ -602,7 +607,7 @@ int enqueue_step(gpuai_searches *s, uint32_t q) {
     SCK(ga::net::forward(s->net, s->fw, reinterpret_cast<const gpuai_board *>(s->leaves.board), 0, s->leaves.sizes,
                          s->ctl + 1, st),
         "network forward on the leaves");
-    leaf_eval_kernel<<<(max_leaves + 255) / 256, 256, 0, st>>>(s->pool, s->leaves, s->fw.logits, s->fw.vraw,
+    leaf_eval_kernel<<<(max_leaves + 255) / 256, 256, 0, st>>>(s->pool, s->leaves, s->fw.logits_b, s->fw.vraw,
                                                                max_leaves);
     backprop_learned_kernel<<<(max_leaves + 255) / 256, 256, 0, st>>>(s->pool, s->tab, s->leaves, s->ppl,
                                                                       max_leaves, s->lrn);
@@ -817,7 +822,7 @@ int gpuai_searches_set_net(gpuai_searches *s, gpuai_net *net, float value_weight
     const size_t L = (size_t)s->slots * s->qmax;
     SCK(dalloc(s, &s->pool.prior, (size_t)s->pool_nodes * kPriors), "prior pool");
     SCK(dalloc(s, &s->leaves.value, L), "leaf values");
-    SCK(ga::net::fwd_alloc(s->fw, (uint32_t)L, s->allocations), "network workspace");
+    SCK(ga::net::fwd_alloc(s->fw, (uint32_t)L, s->allocations, true), "network workspace");
   }
   s->net = net;
   s->lrn.c_puct = c_puct;
