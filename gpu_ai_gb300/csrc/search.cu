@@ -67,6 +67,7 @@ constexpr int kMaxChildren = 64;  // moves per position handled by split_slots
 constexpr uint32_t kUnits = 64;   // learned searches: visit units per leaf slot (score2 = units * (1 + value))
 constexpr uint32_t kPriors = 32;  // stored priors per node (more moves: uniform priors)
 constexpr float kFpuReduction = 0.1f;  // unvisited child's Q = parent's Q - this
+constexpr float kTerminalLeaf = 2.0f;  // leaf value marking a finished game
 
 struct Pool {  // one entry per node
   uint4 *info;   // {first child, nchild | state << 16, visits, score2}
@@ -149,10 +150,13 @@ __global__ void __launch_bounds__(1024) quota_kernel(Table t, uint32_t slots, ui
   }
 }
 
-// Number of children node n would get (its legal moves), 0 for none.
+// Number of children node n would get (its legal moves), 0 for none or when
+// the game is over (a node's terminal flag is set only for roots; a finished
+// game below the root is found here, when it is first to be expanded).
 __device__ int child_count(const Pool &p, int32_t n) {
   const uint4 bv = p.board[n];
   const Board b{bv.x, bv.y, bv.z, bv.w};
+  if (((b.meta >> 8) & 0xffu) >= (uint32_t)kDrawPlies) return 0;
   Side sd;
   make_side(b, sd);
   const int k = count_moves(sd, jumpers(sd));
@@ -171,7 +175,7 @@ __device__ void expand_at(const Pool &p, int32_t n, int32_t base, int k) {
     apply_move(cb, from, to, removed);
     p.board[c] = make_uint4(cb.p1, cb.p2, cb.kings, cb.meta);
     p.parent[c] = n;
-    p.info[c] = make_uint4(0xffffffffu, (board_terminal(cb) ? kTerminal : 0u) << 16, 0u, 0u);
+    p.info[c] = make_uint4(0xffffffffu, 0u, 0u, 0u);
     p.move[c] = (uint32_t)from | ((uint32_t)to << 8) | ((uint32_t)jumps << 16) |
                 ((promotes(b, from, to) ? 1u : 0u) << 24);
     p.removed[c] = removed;
@@ -435,8 +439,9 @@ __global__ void backprop_learned_kernel(Pool p, Table t, Leaves l, uint32_t ppl,
   for (uint32_t k = 0; k < ppl; k++) sum += l.out[(size_t)i * ppl + k];
   const float pm = (float)sum / (float)ppl;
   float x1 = pm;
-  if (!((p.info[leaf].y >> 16) & kTerminal)) {
-    const float v1 = (p.board[leaf].w & 1u) ? -l.value[i] : l.value[i];  // value is for the side to move
+  const float v = l.value[i];
+  if (v <= 1.0f) {  // kTerminalLeaf (> 1): a finished game, whose playouts give the exact result
+    const float v1 = (p.board[leaf].w & 1u) ? -v : v;  // the value is for the side to move
     x1 = lrn.value_weight * v1 + (1.0f - lrn.value_weight) * pm;
   }
   x1 = fminf(1.0f, fmaxf(-1.0f, x1));
@@ -451,23 +456,25 @@ __global__ void backprop_learned_kernel(Pool p, Table t, Leaves l, uint32_t ppl,
 }
 
 // Learned searches: one thread per leaf.  The leaf value (tanh of the value
-// head, for the side to move) and, the first time a node is a leaf, its
-// moves' priors: the softmax of the move logits over its legal (from, to)
-// pairs, a pair's probability shared equally by the moves that have it.
+// head, for the side to move; kTerminalLeaf for a finished game) and, the
+// first time a node is a leaf, its moves' priors: the softmax of the move
+// logits over its legal (from, to) pairs, a pair's probability shared equally
+// by the moves that have it.
 __global__ void leaf_eval_kernel(Pool p, Leaves l, const __nv_bfloat16 *logits, const float *vraw,
                                  uint32_t max_leaves) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= max_leaves || i >= l.sizes[0]) return;
-  l.value[i] = tanhf(vraw[i]);
-  const int32_t n = l.node[i];
-  const uint32_t st = p.info[n].y >> 16;
-  if (st & (kEvaluated | kTerminal)) return;
   const uint4 bv = l.board[i];
   const Board b{bv.x, bv.y, bv.z, bv.w};
   Side sd;
   make_side(b, sd);
   const uint32_t J = jumpers(sd);
   const int k = count_moves(sd, J);
+  const bool over = k == 0 || ((b.meta >> 8) & 0xffu) >= (uint32_t)kDrawPlies;
+  l.value[i] = over ? kTerminalLeaf : tanhf(vraw[i]);
+  const int32_t n = l.node[i];
+  const uint32_t st = p.info[n].y >> 16;
+  if (over || (st & (kEvaluated | kTerminal))) return;
   if (k >= 1 && k <= (int)kPriors) {
     uint16_t pair[kPriors] = {};
     uint8_t of[kPriors];
@@ -547,6 +554,8 @@ struct gpuai_searches {
   gpuai_net *net = nullptr;
   Learned lrn{1.5f, 1.0f};
   ga::net::Fwd fw;
+  cudaStream_t side = nullptr;  // the network's branch of a learned step
+  cudaEvent_t fork = nullptr, join = nullptr;
 };
 
 namespace {
@@ -601,14 +610,24 @@ int enqueue_step(gpuai_searches *s, uint32_t q) {
   a.plies = nullptr;
   a.pos_stream = reinterpret_cast<const uint64_t *>(s->leaves.stream);
   a.dev_sizes = s->leaves.sizes;
-  SCK(launch_playouts(a, s->policy, kPlayoutBlock, s->sms * s->blocks_per_sm, st), "playout kernel launch");
   const uint32_t max_leaves = s->slots * s->qmax;
   if (s->net) {
+    // the network's forward pass and the leaf evaluation do not depend on the
+    // playouts: they run on a second stream and fill the SMs that the playout
+    // kernel's last games leave idle; backprop waits for both
+    SCK(cudaEventRecord(s->fork, st), "fork");
+    SCK(cudaStreamWaitEvent(s->side, s->fork, 0), "fork");
     SCK(ga::net::forward(s->net, s->fw, reinterpret_cast<const gpuai_board *>(s->leaves.board), 0, s->leaves.sizes,
-                         s->ctl + 1, st),
+                         s->ctl + 1, s->side),
         "network forward on the leaves");
-    leaf_eval_kernel<<<(max_leaves + 255) / 256, 256, 0, st>>>(s->pool, s->leaves, s->fw.logits_b, s->fw.vraw,
-                                                               max_leaves);
+    leaf_eval_kernel<<<(max_leaves + 255) / 256, 256, 0, s->side>>>(s->pool, s->leaves, s->fw.logits_b,
+                                                                    s->fw.vraw, max_leaves);
+    SCK(cudaGetLastError(), "leaf evaluation launch");
+    SCK(cudaEventRecord(s->join, s->side), "join");
+  }
+  SCK(launch_playouts(a, s->policy, kPlayoutBlock, s->sms * s->blocks_per_sm, st), "playout kernel launch");
+  if (s->net) {
+    SCK(cudaStreamWaitEvent(st, s->join, 0), "join");
     backprop_learned_kernel<<<(max_leaves + 255) / 256, 256, 0, st>>>(s->pool, s->tab, s->leaves, s->ppl,
                                                                       max_leaves, s->lrn);
   } else {
@@ -688,8 +707,12 @@ void gpuai_searches_destroy(gpuai_searches *s) {
   if (!s) return;
   cudaSetDevice(s->device);
   if (s->stream) cudaStreamSynchronize(s->stream);
+  if (s->side) cudaStreamSynchronize(s->side);
   if (s->graph) cudaGraphExecDestroy(s->graph);
   for (void *p : s->allocations) cudaFree(p);
+  if (s->fork) cudaEventDestroy(s->fork);
+  if (s->join) cudaEventDestroy(s->join);
+  if (s->side) cudaStreamDestroy(s->side);
   if (s->stream) cudaStreamDestroy(s->stream);
   delete s;
 }
@@ -820,6 +843,9 @@ int gpuai_searches_set_net(gpuai_searches *s, gpuai_net *net, float value_weight
   SCK(cudaSetDevice(s->device), "cudaSetDevice");
   if (net && !s->pool.prior) {
     const size_t L = (size_t)s->slots * s->qmax;
+    SCK(cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking), "network stream");
+    SCK(cudaEventCreateWithFlags(&s->fork, cudaEventDisableTiming), "event");
+    SCK(cudaEventCreateWithFlags(&s->join, cudaEventDisableTiming), "event");
     SCK(dalloc(s, &s->pool.prior, (size_t)s->pool_nodes * kPriors), "prior pool");
     SCK(dalloc(s, &s->leaves.value, L), "leaf values");
     SCK(ga::net::fwd_alloc(s->fw, (uint32_t)L, s->allocations, true), "network workspace");
