@@ -96,10 +96,13 @@ __global__ void __launch_bounds__(BLOCK) playout_kernel(PlayoutArgs a) {
     // Uniform random policy: at most one draw per ply, so Philox blocks are
     // generated for the whole warp every fourth iteration (DrawRing keeps four
     // or more draws buffered) and new games start on those iterations too.
-    // Plies whose capture can be extended (about 3% of plies) are deferred to
-    // every kSearchPeriod-th iteration, so that the lanes needing the longer
-    // capture code run it together and the per-iteration code stays
-    // branch-free for the others.
+    // Plies whose capture can be extended take longer code: men's multi-jumps
+    // (about 2.6% of plies) are deferred to every kMenPeriod-th iteration and
+    // plies where a king's capture can continue (about 0.7%, the costlier
+    // depth-first search) to every kKingPeriod-th, so that the lanes needing
+    // that code run it together and the other iterations stay branch-free.
+    // Once the work counter is exhausted, a warp with kSparseLanes or fewer
+    // games defers nothing: its few games are latency-bound.
     //
     // Once the work counter is exhausted, every kCompactPeriod-th iteration the
     // block packs its unfinished games (board, random-stream state, counters)
@@ -117,7 +120,7 @@ __global__ void __launch_bounds__(BLOCK) playout_kernel(PlayoutArgs a) {
     __syncthreads();
     DrawRing rs;
     rs.start(0, 0, 0);
-    bool pending = false;
+    uint32_t pend = 0;  // deferred ply: 0 none, 1 men's multi-jump, 2 king capture search
     auto pick = [&](uint32_t n) { return rs.pick(n); };
     for (uint32_t it = 0;; ++it) {
       if ((it & 3u) == 0) {
@@ -130,25 +133,23 @@ __global__ void __launch_bounds__(BLOCK) playout_kernel(PlayoutArgs a) {
         }
         if (have) rs.refill();
       }
+      const bool sparse = exhausted && __popc(__ballot_sync(kFull, have)) <= kSparseLanes;
+      const bool men_ok = sparse || (it & (kMenPeriod - 1u)) == kMenPhase;
+      const bool king_ok = sparse || (it & (kKingPeriod - 1u)) == kKingPhase;
       do {
         if (!have) break;
-        int n;
-        if (pending) {
-          if ((it & (kSearchPeriod - 1u)) != 0) break;
-          pending = false;
-          n = play_ply_fast<false>(b, pick);
-        } else {
-          if (((b.meta >> 8) & 0xffu) >= (uint32_t)kDrawPlies) {
-            a.out[j] = 0;
-            have = false;
-            break;
-          }
-          n = play_ply_fast<true>(b, pick);
-          if (n == kNeedSearch) {
-            pending = true;
-            break;
-          }
+        if ((pend == 1u && !men_ok) || (pend == 2u && !king_ok)) break;  // still deferred
+        if (((b.meta >> 8) & 0xffu) >= (uint32_t)kDrawPlies) {
+          a.out[j] = 0;
+          have = false;
+          break;
         }
+        const int n = play_ply_sched(b, pick, men_ok, king_ok);
+        if (n == kNeedMen || n == kNeedKing) {
+          pend = n == kNeedMen ? 1u : 2u;
+          break;
+        }
+        pend = 0;
         if (n > 0 && ++game_plies <= kMaxPlies) {
           plies_here++;
           break;
@@ -184,7 +185,7 @@ __global__ void __launch_bounds__(BLOCK) playout_kernel(PlayoutArgs a) {
       if ((total + 31u) / 32u >= busy_warps) continue;  // packing would free no warp
       if (have) {
         const uint32_t slot = before + __popc(m & ((1u << lane) - 1u));
-        const uint32_t v[kWords] = {b.p1, b.p2, b.kings, b.meta, j, game_plies, pending ? 1u : 0u,
+        const uint32_t v[kWords] = {b.p1, b.p2, b.kings, b.meta, j, game_plies, pend,
                                     rs.a0, rs.a1, rs.a2, rs.a3, rs.b0, rs.b1, rs.b2, rs.b3, rs.k, rs.avail};
 #pragma unroll
         for (int q = 0; q < kWords; q++) s_slot[q][slot] = v[q];
@@ -196,7 +197,7 @@ __global__ void __launch_bounds__(BLOCK) playout_kernel(PlayoutArgs a) {
         b.p1 = s_slot[0][t]; b.p2 = s_slot[1][t]; b.kings = s_slot[2][t]; b.meta = s_slot[3][t];
         j = s_slot[4][t];
         game_plies = s_slot[5][t];
-        pending = s_slot[6][t] != 0;
+        pend = s_slot[6][t];
         rs.start(a.seed, stream_of(a, position_of(a, j), j), 0);  // then the buffered draws and counter
         rs.a0 = s_slot[7][t]; rs.a1 = s_slot[8][t]; rs.a2 = s_slot[9][t]; rs.a3 = s_slot[10][t];
         rs.b0 = s_slot[11][t]; rs.b1 = s_slot[12][t]; rs.b2 = s_slot[13][t]; rs.b3 = s_slot[14][t];

@@ -15,7 +15,6 @@ constexpr uint32_t kStatusPlyCap = 4u;    // playout exceeded kMaxPlies (cannot 
 
 constexpr int kPlayoutBlock = 256;        // default threads per block
 constexpr uint32_t kMaxPlies = 4096;
-constexpr uint32_t kSearchPeriod = 8;     // iterations between deferred capture searches (power of 2, >= 4)
 constexpr uint32_t kCompactPeriod = 16;   // iterations between block compactions once the work runs out (power of 2, >= 4)
 
 struct PlayoutArgs {

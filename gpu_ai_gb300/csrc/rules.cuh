@@ -178,7 +178,7 @@ GA_HD int capture_walk(const Side &s, int o, Leaf &&leaf) {
   if (rem == 0) return 0;
   for (;;) {
     if (rem) {
-      int j = ctz(rem);
+      int j = (int)((0x12131210u >> (2u * rem)) & 3u);  // lowest set bit of the 4-bit set
       rem &= rem - 1;
       int d = dir_of(j, king, s.turn);
       if (depth >= kMaxDepth) return -1;
@@ -421,6 +421,71 @@ GA_HD int nth_bit4(uint32_t dm, uint32_t rem) {
   return (int)((word >> (2u * (idx & 15u))) & 3u);
 }
 
+// Byte-wise population counts: byte k of the result = popcount of byte k of x.
+GA_HD uint32_t popc8(uint32_t x) {
+  x = x - ((x >> 1) & 0x55555555u);
+  x = (x & 0x33333333u) + ((x >> 2) & 0x33333333u);
+  return (x + (x >> 4)) & 0x0F0F0F0Fu;
+}
+
+// Bits 0..3 of x spread to bits 0, 8, 16, 24 (x < 16).
+GA_HD uint32_t spread4(uint32_t x) { return (x * 0x00204081u) & 0x01010101u; }
+
+// Number of bytes k of P with P_k <= i, where the bytes of P are
+// non-decreasing prefix sums below 128 and i < 128.  No byte borrows from its
+// neighbour: each byte computes (0x80 | i) - P_k >= 1.
+GA_HD uint32_t bytes_le(uint32_t P, uint32_t i) {
+  const uint32_t D = ((i * 0x01010101u) | 0x80808080u) - P;
+  return (((D & 0x80808080u) >> 7) * 0x01010101u) >> 24;
+}
+
+// Move i of the list whose per-direction source masks are M0..M3 (a square's
+// moves in one direction each; squares ascending, within a square the
+// directions ascending, or descending for a man's captures, which search
+// dc = -1 first).  Returns the source square, the destination square and the
+// captured squares.  The square is found with byte-wise prefix sums of the
+// per-square move counts instead of a search over prefix popcounts, and the
+// direction from the prefix of the square's direction bits: a short chain of
+// full-rate integer operations.  Every square holds at most four moves and
+// the list at most 48, so every prefix sum fits a byte below 128.
+GA_HD void nth_move(uint32_t M0, uint32_t M1, uint32_t M2, uint32_t M3, uint32_t i, bool capture, uint32_t men,
+                    int &from, int &to, uint32_t &removed) {
+  // per-square move counts (0..4) as three bit planes
+  const uint32_t a0 = M0 ^ M1, a1 = M0 & M1, b0 = M2 ^ M3, b1 = M2 & M3;
+  const uint32_t S0 = a0 ^ b0, k0 = a0 & b0;
+  const uint32_t S1 = a1 ^ b1 ^ k0, S2 = (a1 & b1) | (k0 & (a1 ^ b1));
+  // inclusive prefix sums over the four bytes (eight squares each)
+  const uint32_t P = (popc8(S0) + 2u * popc8(S1) + 4u * popc8(S2)) * 0x01010101u;
+  const uint32_t g = bytes_le(P, i);
+  const uint32_t sh = 8u * g;
+  const uint32_t rem = i - (((P << 8) >> sh) & 0xffu);
+  // the byte's two halves (four squares each): counts per square as bytes
+  const uint32_t e0 = S0 >> sh, e1 = S1 >> sh, e2 = S2 >> sh;
+  const uint32_t Qlo = spread4(e0 & 15u) + 2u * spread4(e1 & 15u) + 4u * spread4(e2 & 15u);
+  const uint32_t Qhi = spread4((e0 >> 4) & 15u) + 2u * spread4((e1 >> 4) & 15u) + 4u * spread4((e2 >> 4) & 15u);
+  const uint32_t Rlo = Qlo * 0x01010101u;
+  const uint32_t tlo = Rlo >> 24;
+  const bool hi = rem >= tlo;
+  const uint32_t Q = hi ? Qhi : Qlo;
+  const uint32_t R = Q * 0x01010101u;
+  const uint32_t rem2 = hi ? rem - tlo : rem;
+  const uint32_t q = bytes_le(R, rem2);
+  const uint32_t sq = sh + (hi ? 4u : 0u) + q;
+  const uint32_t r0 = rem2 - (((R << 8) >> (8u * q)) & 0xffu);  // rank among the square's moves
+  const uint32_t cnt = (Q >> (8u * q)) & 0xffu;
+  const uint32_t x0 = (M0 >> sq) & 1u, x1 = (M1 >> sq) & 1u, x2 = (M2 >> sq) & 1u;
+  const uint32_t r = (capture && ((men >> sq) & 1u)) ? cnt - 1u - r0 : r0;
+  const uint32_t c01 = x0 + x1;
+  // direction = the r-th set bit of (x0, x1, x2, x3)
+  const uint32_t d = (uint32_t)(r >= x0) + (uint32_t)(r >= c01) + (uint32_t)(r >= c01 + x2);
+  const uint32_t sd = 8u * d;
+  const int s = (int)sq;
+  const int mid = s + (int)((0x00010809u >> sd) & 0xffu) - 5 + (((s >> 2) & 1) ^ 1);  // one step along d
+  from = s;
+  to = capture ? s + (int)((0x00021012u >> sd) & 0xffu) - 9 : mid;
+  removed = capture ? 1u << mid : 0u;
+}
+
 // Squares of the side to move whose capture can continue after the first
 // jump (they need the depth-first search); J[d] are the first-jump sources.
 GA_HD uint32_t continuing_sources(const Side &s, const uint32_t J[4]) {
@@ -453,7 +518,34 @@ GA_HD int play_ply(Board &b, Pick &&pick) {
   if (Jall) {
     const uint32_t men = s.own & ~s.ownK;
     const uint32_t X = continuing_sources(s, J);
-    int n = popc(J[0] & ~X) + popc(J[1] & ~X) + popc(J[2] & ~X) + popc(J[3] & ~X);
+    const uint32_t M0 = J[0] & ~X, M1 = J[1] & ~X, M2 = J[2] & ~X, M3 = J[3] & ~X;
+    int n = popc(M0) + popc(M1) + popc(M2) + popc(M3);
+    if (X != 0 && (X & (X - 1u)) == 0) {
+      // One square x whose capture can continue (almost every such ply): its
+      // sequences sit between the single jumps of the squares below x and
+      // those above it, so only x is walked, once to count and once to select.
+      const int x = popc(X - 1u);
+      const uint32_t below = X - 1u;
+      const uint32_t nb = (uint32_t)(popc(M0 & below) + popc(M1 & below) + popc(M2 & below) + popc(M3 & below));
+      const int c = capture_walk(s, x, [](int, uint32_t, int, uint32_t) { return false; });
+      if (c < 0) return -1;
+      n += c;
+      const uint32_t i = pick((uint32_t)n);
+      int from = x, to = x;
+      uint32_t removed = 0;
+      if (i - nb < (uint32_t)c) {  // i in [nb, nb + c): a sequence of x
+        uint32_t want = i - nb;
+        capture_walk(s, x, [&](int t, uint32_t rm, int, uint32_t) {
+          if (want == 0) { to = t; removed = rm; return true; }
+          want--;
+          return false;
+        });
+      } else {
+        nth_move(M0, M1, M2, M3, i < nb ? i : i - (uint32_t)c, true, men, from, to, removed);
+      }
+      apply_move(b, from, to, removed);
+      return n;
+    }
     uint32_t cache = 0;  // 8-bit sequence counts of the first four searched squares
     int q = 0;
     for (uint32_t m = X; m; m &= m - 1) {
@@ -613,17 +705,30 @@ GA_HD int play_ply_men_multi(Board &b, const Side &s, const uint32_t J[4], Pick 
   return -1;  // unreachable: i < n
 }
 
-constexpr int kNeedSearch = -2;
+constexpr int kNeedSearch = -2;  // a men's multi-jump ply was deferred (kNeedMen)
+constexpr int kNeedMen = -2;
+constexpr int kNeedKing = -3;     // a ply where a king's capture can continue was deferred
+
+// Deferred-ply schedule of the uniform random playout kernel (iteration it of
+// its warp loop): Philox blocks are generated on it % 4 == 0, men's
+// multi-jumps are played on it % kMenPeriod == kMenPhase, king capture
+// searches on it % kKingPeriod == kKingPhase (powers of 2, phases away from
+// the refill and the compaction iterations); once the work runs out, a warp
+// with at most kSparseLanes games defers nothing.
+constexpr uint32_t kMenPeriod = 4, kMenPhase = 2;
+constexpr uint32_t kKingPeriod = 16, kKingPhase = 6;
+constexpr uint32_t kSparseLanes = 4;
 
 // One uniformly random ply, branch-free for direct moves and for captures
 // that cannot be extended (the common cases).  Positions where some capture
-// can continue take the bit-sliced men's tree (play_ply_men_multi) or the
-// depth-first search (play_ply); with DEFER they instead return kNeedSearch
-// without touching the board or the stream, and the caller runs
-// play_ply_fast<false> later.  Same move list order, same index -> move map as
-// play_ply.
-template <bool DEFER = false, class Pick>
-GA_HD int play_ply_fast(Board &b, Pick &&pick) {
+// can continue take the bit-sliced men's tree (play_ply_men_multi) when only
+// men continue, or the depth-first search with the cycle check (play_ply)
+// when a king does.  A caller that batches these rarer plies passes
+// men_now / king_now = false: the ply then returns kNeedMen / kNeedKing
+// without touching the board or the stream, and is played by a later call
+// that allows it.  Same move list order, same index -> move map as play_ply.
+template <class Pick>
+GA_HD int play_ply_sched(Board &b, Pick &&pick, bool men_now, bool king_now) {
   Side s;
   make_side(b, s);
   const uint32_t men = s.own & ~s.ownK;
@@ -639,8 +744,11 @@ GA_HD int play_ply_fast(Board &b, Pick &&pick) {
                       jump2<3>(J3 & s.ownK);
   const uint32_t cont_k = lk & jall, cont_m = lm & jf;
   if (cont_k | cont_m) {
-    if (DEFER) return kNeedSearch;
-    if (cont_k) return play_ply(b, pick);  // a king can continue: depth-first search with the cycle check
+    if (cont_k) {
+      if (!king_now) return kNeedKing;
+      return play_ply(b, pick);  // a king can continue: depth-first search with the cycle check
+    }
+    if (!men_now) return kNeedMen;
     // only men continue: counted on the bit-sliced continuation tree
     const uint32_t J[4] = {J0, J1, J2, J3};
     return s.turn ? play_ply_men_multi<3, 2>(b, s, J, pick) : play_ply_men_multi<1, 0>(b, s, J, pick);
@@ -652,29 +760,18 @@ GA_HD int play_ply_fast(Board &b, Pick &&pick) {
   const int n = popc(M0) + popc(M1) + popc(M2) + popc(M3);
   if (n == 0) return 0;
   const uint32_t i = pick((uint32_t)n);
-  // square of move i: the largest x with (moves from squares < x) <= i
-  uint32_t lo = 0, clo = 0;
-GA_UNROLL
-  for (uint32_t st = 16; st >= 1; st >>= 1) {
-    const uint32_t mid = lo + st;
-    const uint32_t L = (1u << mid) - 1u;
-    const uint32_t c = (uint32_t)(popc(M0 & L) + popc(M1 & L) + popc(M2 & L) + popc(M3 & L));
-    const bool le = c <= i;
-    lo = le ? mid : lo;
-    clo = le ? c : clo;
-  }
-  const int sq = (int)lo;
-  const uint32_t rem = i - clo;
-  const uint32_t dm = ((M0 >> sq) & 1u) | (((M1 >> sq) & 1u) << 1) | (((M2 >> sq) & 1u) << 2) |
-                      (((M3 >> sq) & 1u) << 3);
-  // men search captures dc=-1 first: the reverse of the ascending direction order
-  const bool reverse = capture && ((men >> sq) & 1u);
-  const int d = nth_bit4(dm, reverse ? (uint32_t)popc(dm) - 1u - rem : rem);
-  const int tj = sq + jump_off(d), ts = sq + step_off(sq, d);
-  const int to = capture ? tj : ts;
-  const uint32_t removed = capture ? (1u << mid_square(sq, tj)) : 0u;
-  apply_move(b, sq, to, removed);
+  int from, to;
+  uint32_t removed;
+  nth_move(M0, M1, M2, M3, i, capture, men, from, to, removed);
+  apply_move(b, from, to, removed);
   return n;
+}
+
+// play_ply_sched with every rarer ply deferred (DEFER, returning kNeedMen or
+// kNeedKing) or played at once.
+template <bool DEFER = false, class Pick>
+GA_HD int play_ply_fast(Board &b, Pick &&pick) {
+  return play_ply_sched(b, pick, !DEFER, !DEFER);
 }
 
 // Random draws of one stream buffered eight at a time, so that a warp can

@@ -65,28 +65,29 @@ int rh_playout(const uint32_t *pos, uint64_t seed, uint64_t id, int policy, uint
 }
 
 // The same playout with the uniform-random kernel's schedule: Philox blocks
-// generated every fourth iteration (DrawRing), plies whose capture can be
-// extended deferred to every eighth iteration, as the warp loop does.
-int rh_playout_ring(const uint32_t *pos, uint64_t seed, uint64_t id, uint32_t *plies, uint32_t *draws) {
+// generated every fourth iteration (DrawRing), men's multi-jumps and king
+// capture searches deferred to their own iterations, as the warp loop does;
+// from iteration sparse_from on nothing is deferred (the kernel's schedule for
+// a warp left with few games).
+int rh_playout_ring(const uint32_t *pos, uint64_t seed, uint64_t id, uint32_t sparse_from, uint32_t *plies,
+                    uint32_t *draws) {
   Board b = load(pos);
   DrawRing rs;
   rs.start(seed, id, 0);
   auto pick = [&](uint32_t n) { return rs.pick(n); };
   uint32_t p = 0;
   int outcome = 0;
-  bool pending = false;
+  uint32_t pend = 0;
   for (uint32_t it = 0;; ++it) {
     if ((it & 3u) == 0) rs.refill();
-    int n;
-    if (pending) {
-      if ((it & 7u) != 0) continue;
-      pending = false;
-      n = play_ply_fast<false>(b, pick);
-    } else {
-      if (((b.meta >> 8) & 0xffu) >= (uint32_t)kDrawPlies) { outcome = 0; break; }
-      n = play_ply_fast<true>(b, pick);
-      if (n == kNeedSearch) { pending = true; continue; }
-    }
+    const bool sparse = it >= sparse_from;
+    const bool men_ok = sparse || (it & (kMenPeriod - 1u)) == kMenPhase;
+    const bool king_ok = sparse || (it & (kKingPeriod - 1u)) == kKingPhase;
+    if ((pend == 1u && !men_ok) || (pend == 2u && !king_ok)) continue;
+    if (((b.meta >> 8) & 0xffu) >= (uint32_t)kDrawPlies) { outcome = 0; break; }
+    const int n = play_ply_sched(b, pick, men_ok, king_ok);
+    if (n == kNeedMen || n == kNeedKing) { pend = n == kNeedMen ? 1u : 2u; continue; }
+    pend = 0;
     if (n == 0) { outcome = (b.meta & 1u) ? 1 : -1; break; }
     if (n < 0) { outcome = -100; break; }
     p++;
