@@ -275,8 +275,10 @@ def run_ours(args):
     value = world * args.steps * TOTAL / kern_s_max
 
     # ---- end to end through the public host-buffer call
-    h2d = N_POS * 16 + (N_POS + 1) * 4
-    d2h = TOTAL + 16
+    # gpuai_playouts copies [boards | control block] up, the outcomes and the
+    # control block down (equal repetitions need no offsets)
+    h2d = N_POS * 16 + 16
+    d2h = 16 + TOTAL
     for k in range(2):
         eng.playouts(positions, reps, seed=0xE2E, stream_base=base + k * TOTAL)
     barrier(world)

@@ -107,8 +107,10 @@ struct gpuai_ctx {
   int max_blocks_per_sm[3] = {0, 0, 0};
   int layout[3] = {ga::kLayoutThread, ga::kLayoutThread, ga::kLayoutThread};
   Control *ctl = nullptr;  // device
-  DevBuf d_in, d_off, d_out, d_aux;
-  HostBuf h_in, h_out;
+  Control last_host{};      // control block of the last host-buffer call, as read back
+  bool last_was_host = false;
+  DevBuf d_in, d_aux;  // staging of host-buffer calls; move lists
+  HostBuf h_in;
   std::mutex mu;
 };
 
@@ -137,11 +139,13 @@ int grid_for(gpuai_ctx *ctx, int policy, uint32_t total) {
   return (int)(g < 1 ? 1 : g);
 }
 
-// Launch on device buffers; ctx->mu held, device current.
+// Launch on device buffers; ctx->mu held, device current.  ctl is the work
+// counter / status / ply block the launch uses; it is zeroed here unless the
+// caller has already zeroed it on the stream (zeroed = true).
 int launch_device(gpuai_ctx *ctx, const gpuai_board *d_pos, const uint32_t *d_off, uint32_t npos,
                   uint32_t uniform_reps, uint32_t total, uint64_t seed, uint64_t stream_base,
-                  int32_t policy, int8_t *d_out, cudaStream_t s) {
-  CK(cudaMemsetAsync(ctx->ctl, 0, sizeof(Control), s), "reset work counter");
+                  int32_t policy, int8_t *d_out, cudaStream_t s, Control *ctl, bool zeroed) {
+  if (!zeroed) CK(cudaMemsetAsync(ctl, 0, sizeof(Control), s), "reset work counter");
   ga::PlayoutArgs a;
   a.pos = reinterpret_cast<const ga::Board *>(d_pos);
   a.offsets = d_off;
@@ -151,9 +155,9 @@ int launch_device(gpuai_ctx *ctx, const gpuai_board *d_pos, const uint32_t *d_of
   a.seed = seed;
   a.stream_base = stream_base;
   a.out = d_out;
-  a.counter = &ctx->ctl->counter;
-  a.status = &ctx->ctl->status;
-  a.plies = &ctx->ctl->plies;
+  a.counter = &ctl->counter;
+  a.status = &ctl->status;
+  a.plies = &ctl->plies;
   CK(ga::launch_playouts(a, policy, ctx->block[policy], grid_for(ctx, policy, total), s, ctx->layout[policy]),
      "playout kernel launch");
   return GPUAI_OK;
@@ -212,11 +216,8 @@ void gpuai_destroy(gpuai_ctx *ctx) {
   cudaSetDevice(ctx->device);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   ctx->d_in.release();
-  ctx->d_off.release();
-  ctx->d_out.release();
   ctx->d_aux.release();
   ctx->h_in.release();
-  ctx->h_out.release();
   if (ctx->ctl) cudaFree(ctx->ctl);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
@@ -305,34 +306,50 @@ int gpuai_playouts(gpuai_ctx *ctx, const gpuai_board *pos, const uint32_t *reps,
   std::lock_guard<std::mutex> lock(ctx->mu);
   if ((rc = set_device(ctx))) return rc;
   cudaStream_t s = ctx->stream;
+  // Device layout [boards | offsets | control | outcomes]: the control block
+  // (work counter, status, plies) travels zeroed with the inputs in one copy
+  // from pinned staging; the outcomes are copied straight into the caller's
+  // buffer (a device-to-host copy into pageable memory is as fast as into
+  // pinned memory on a coherent CPU-GPU link, and spares a host memcpy).
+  // Equal repetitions (or none) need no offsets: the kernel divides instead.
+  uint32_t uniform = 1;
+  if (reps) {
+    uniform = reps[0];
+    for (uint32_t p = 1; p < npos && uniform; p++)
+      if (reps[p] != uniform) uniform = 0;
+    if (uniform) reps = nullptr;
+  }
   const size_t bytes_pos = sizeof(gpuai_board) * (size_t)npos;
   const size_t bytes_off = reps ? sizeof(uint32_t) * ((size_t)npos + 1) : 0;
-  CK(ctx->h_in.reserve(bytes_pos + bytes_off), "pinned staging");
-  CK(ctx->h_out.reserve((size_t)total), "pinned staging");
-  CK(ctx->d_in.reserve(bytes_pos), "device buffer");
-  CK(ctx->d_out.reserve((size_t)total), "device buffer");
-  std::memcpy(ctx->h_in.p, pos, bytes_pos);
-  uint32_t *h_off = nullptr;
+  const size_t ctl_at = (bytes_pos + bytes_off + 15) & ~(size_t)15;
+  const size_t out_at = ctl_at + sizeof(Control);
+  const size_t bytes_all = out_at + (size_t)total;
+  CK(ctx->h_in.reserve(out_at), "pinned staging");
+  CK(ctx->d_in.reserve(bytes_all), "device buffer");
+  char *h = static_cast<char *>(ctx->h_in.p);
+  char *d = static_cast<char *>(ctx->d_in.p);
+  std::memcpy(h, pos, bytes_pos);
   if (reps) {
-    CK(ctx->d_off.reserve(bytes_off), "device buffer");
-    h_off = reinterpret_cast<uint32_t *>(static_cast<char *>(ctx->h_in.p) + bytes_pos);
+    uint32_t *h_off = reinterpret_cast<uint32_t *>(h + bytes_pos);
     h_off[0] = 0;
     for (uint32_t p = 0; p < npos; p++) h_off[p + 1] = h_off[p] + reps[p];
   }
-  CK(cudaMemcpyAsync(ctx->d_in.p, ctx->h_in.p, bytes_pos, cudaMemcpyHostToDevice, s), "H2D boards");
-  if (reps)
-    CK(cudaMemcpyAsync(ctx->d_off.p, h_off, bytes_off, cudaMemcpyHostToDevice, s), "H2D offsets");
-  rc = launch_device(ctx, static_cast<const gpuai_board *>(ctx->d_in.p),
-                     reps ? static_cast<const uint32_t *>(ctx->d_off.p) : nullptr, npos, 1,
-                     (uint32_t)total, seed, stream_base, policy, static_cast<int8_t *>(ctx->d_out.p), s);
+  std::memset(h + bytes_pos + bytes_off, 0, out_at - (bytes_pos + bytes_off));
+  CK(cudaMemcpyAsync(d, h, out_at, cudaMemcpyHostToDevice, s), "H2D boards");
+  Control *d_ctl = reinterpret_cast<Control *>(d + ctl_at);
+  rc = launch_device(ctx, reinterpret_cast<const gpuai_board *>(d),
+                     reps ? reinterpret_cast<const uint32_t *>(d + bytes_pos) : nullptr, npos, uniform, (uint32_t)total,
+                     seed, stream_base, policy, reinterpret_cast<int8_t *>(d + out_at), s, d_ctl, true);
   if (rc) return rc;
-  Control ctl_h;
-  CK(cudaMemcpyAsync(ctx->h_out.p, ctx->d_out.p, (size_t)total, cudaMemcpyDeviceToHost, s), "D2H outcomes");
-  CK(cudaMemcpyAsync(&ctl_h, ctx->ctl, sizeof(Control), cudaMemcpyDeviceToHost, s), "D2H status");
+  CK(cudaMemcpyAsync(out, d + out_at, (size_t)total, cudaMemcpyDeviceToHost, s), "D2H outcomes");
+  CK(cudaMemcpyAsync(h + ctl_at, d + ctl_at, sizeof(Control), cudaMemcpyDeviceToHost, s), "D2H status");
   CK(cudaStreamSynchronize(s), "playout kernel");
+  Control ctl_h;
+  std::memcpy(&ctl_h, h + ctl_at, sizeof ctl_h);
+  ctx->last_host = ctl_h;
+  ctx->last_was_host = true;
   if (ctl_h.status)
     return fail(GPUAI_ERR_LIMIT, "playout kernel status 0x%x (capture depth / ply limit)", ctl_h.status);
-  std::memcpy(out, ctx->h_out.p, (size_t)total);
   return GPUAI_OK;
 }
 
@@ -350,8 +367,9 @@ int gpuai_playouts_device(gpuai_ctx *ctx, const gpuai_board *d_pos, const uint32
   int rc = set_device(ctx);
   if (rc) return rc;
   cudaStream_t s = static_cast<cudaStream_t>(stream);  // NULL: the legacy default stream
+  ctx->last_was_host = false;
   return launch_device(ctx, d_pos, d_offsets, npos, uniform_reps, total, seed, stream_base, policy,
-                       d_out, s);
+                       d_out, s, ctx->ctl, false);
 }
 
 int gpuai_status(gpuai_ctx *ctx, uint32_t *status, uint64_t *plies) {
@@ -361,7 +379,8 @@ int gpuai_status(gpuai_ctx *ctx, uint32_t *status, uint64_t *plies) {
   if (rc) return rc;
   Control c;
   CK(cudaDeviceSynchronize(), "synchronise before status read");
-  CK(cudaMemcpy(&c, ctx->ctl, sizeof c, cudaMemcpyDeviceToHost), "D2H status");
+  if (ctx->last_was_host) c = ctx->last_host;
+  else CK(cudaMemcpy(&c, ctx->ctl, sizeof c, cudaMemcpyDeviceToHost), "D2H status");
   if (status) *status = c.status;
   if (plies) *plies = c.plies;
   return GPUAI_OK;

@@ -44,8 +44,9 @@ __device__ __forceinline__ Board load_board(const Board *p) {
 // Returns true for lanes that got a playout (index in j).
 __device__ __forceinline__ bool claim(const PlayoutArgs &a, bool have, uint32_t &j, bool &exhausted,
                                       uint32_t lane) {
+  if (exhausted) return false;  // warp-uniform
   const uint32_t need = __ballot_sync(kFull, !have);
-  if (!need || exhausted) return false;
+  if (!need) return false;
   const uint32_t cnt = __popc(need);
   const uint32_t leader = __ffs(need) - 1;
   uint32_t base = 0;
@@ -120,7 +121,8 @@ __global__ void __launch_bounds__(BLOCK) playout_kernel(PlayoutArgs a) {
     __syncthreads();
     DrawRing rs;
     rs.start(0, 0, 0);
-    uint32_t pend = 0;  // deferred ply: 0 none, 1 men's multi-jump, 2 king capture search
+    uint32_t pend = 0;    // deferred ply: 0 none, 1 men's multi-jump, 2 king capture search
+    bool sparse = false;  // warp-uniform: the work ran out and the warp holds kSparseLanes games or fewer
     auto pick = [&](uint32_t n) { return rs.pick(n); };
     for (uint32_t it = 0;; ++it) {
       if ((it & 3u) == 0) {
@@ -133,7 +135,6 @@ __global__ void __launch_bounds__(BLOCK) playout_kernel(PlayoutArgs a) {
         }
         if (have) rs.refill();
       }
-      const bool sparse = exhausted && __popc(__ballot_sync(kFull, have)) <= kSparseLanes;
       const bool men_ok = sparse || (it & (kMenPeriod - 1u)) == kMenPhase;
       const bool king_ok = sparse || (it & (kKingPeriod - 1u)) == kKingPhase;
       do {
@@ -161,8 +162,12 @@ __global__ void __launch_bounds__(BLOCK) playout_kernel(PlayoutArgs a) {
       } while (false);
 
       if ((it & (kCompactPeriod - 1u)) != kCompactPeriod - 1u) {
-        // a warp with no game left skips ahead to the block's next compaction point
-        if (exhausted && !__any_sync(kFull, have)) it = (it | (kCompactPeriod - 1u)) - 1u;
+        if (exhausted) {
+          const uint32_t live = __ballot_sync(kFull, have);
+          sparse = __popc(live) <= kSparseLanes;
+          // a warp with no game left skips ahead to the block's next compaction point
+          if (!live) it = (it | (kCompactPeriod - 1u)) - 1u;
+        }
         continue;
       }
       const uint32_t parity = (it / kCompactPeriod) & 1u;
@@ -182,6 +187,7 @@ __global__ void __launch_bounds__(BLOCK) playout_kernel(PlayoutArgs a) {
       }
       if (total == 0) break;
       exhausted = true;
+      sparse = __popc(m) <= kSparseLanes;
       if ((total + 31u) / 32u >= busy_warps) continue;  // packing would free no warp
       if (have) {
         const uint32_t slot = before + __popc(m & ((1u << lane) - 1u));
@@ -192,6 +198,7 @@ __global__ void __launch_bounds__(BLOCK) playout_kernel(PlayoutArgs a) {
       }
       __syncthreads();
       have = threadIdx.x < total;
+      sparse = total <= warp * 32u + kSparseLanes;  // this warp now holds min(32, total - 32 * warp) games
       if (have) {
         const uint32_t t = threadIdx.x;
         b.p1 = s_slot[0][t]; b.p2 = s_slot[1][t]; b.kings = s_slot[2][t]; b.meta = s_slot[3][t];

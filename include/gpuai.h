@@ -84,8 +84,8 @@ int gpuai_playouts_device(gpuai_ctx *ctx, const gpuai_board *d_pos, const uint32
                           uint32_t npos, uint32_t uniform_reps, uint32_t total, uint64_t seed,
                           uint64_t stream_base, int32_t policy, int8_t *d_out, void *stream);
 
-/* Status word and ply count of the last device-side playout launch (reads
- * device memory; synchronises the context's stream).  status 0 = fine. */
+/* Status word and ply count of the context's last playout call, host-buffer
+ * or device-side (synchronises the device first).  status 0 = fine. */
 int gpuai_status(gpuai_ctx *ctx, uint32_t *status, uint64_t *plies);
 
 /* Legal move lists of n boards, in the reference's State::genMoves order
