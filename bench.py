@@ -372,6 +372,37 @@ def run_searches(args):
     print(json.dumps(line), flush=True)
 
 
+def run_mcts(args):
+    """Host UCT searches with GPU leaf batches (the reference's MCTSPlayer
+    worker loop, src/player.cpp:134-150): 32 seeded positions at 10-40 random
+    plies, --ms-per-position of search each, leaf batches of 16K-64K slots x
+    --playouts-per-leaf playouts; plain random playouts against the
+    eps-greedy and the reference-heuristic playout policies.  Up to 16
+    searches run at once, one host thread, playout driver and CUDA stream
+    each.  Runs gpu_ai_gb300/lib/run_ai -m mcts_bench (the host tree is C++)."""
+    exe = os.path.join(ROOT, "gpu_ai_gb300", "lib", "run_ai")
+    if not os.path.exists(exe):
+        raise RuntimeError(f"{exe} is missing: build it with gpu_ai_gb300.build.build()")
+    cmd = [exe, "-m", "mcts_bench", "-n", "32", "--seed", "2016", "--ms-per-move", str(args.ms_per_position),
+           "--leaves-min", "16384", "--leaves-max", "65536", "--playouts-per-leaf", str(args.playouts_per_leaf)]
+    res = {}
+    for name, drv in (("plain", "device"), ("eps_greedy", "device_eps_greedy"), ("ref_heuristic", "device_heuristic")):
+        r = subprocess.run(cmd + ["-1", drv], capture_output=True, text=True, check=True)
+        line = [x for x in r.stdout.splitlines() if x.startswith("MCTS_BENCH ")][-1]
+        res[name] = json.loads(line[len("MCTS_BENCH "):])
+    p = res["plain"]
+    print(json.dumps({
+        "metric": "checkers playouts/sec, host UCT searches with GPU leaf batches", "value": p["playouts_per_s"],
+        "unit": UNIT, "higher_is_better": True, "n_gpus": 1, "dtype": "u32", "data": "synthetic (seeded positions)",
+        "config": {"workload": f"32 positions (10-40 random plies, seed 2016), {args.ms_per_position} ms of host UCT "
+                               f"search each, leaf batches of 16K-64K slots x {args.playouts_per_leaf} playouts, "
+                               f"up to 16 searches at once",
+                   "tree": "host C++ GameTree, UCB1 c=sqrt(2)"},
+        "threads": p["threads"], "driver_share_of_search_time": p["driver_share"],
+        "plain": p, "eps_greedy": res["eps_greedy"], "ref_heuristic": res["ref_heuristic"],
+    }), flush=True)
+
+
 def quick_net(args):
     """The network file given with --net, or one trained here on 1M self-play
     positions with 1,024-playout labels (a few seconds)."""
@@ -552,7 +583,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--block", type=int, default=0, help="threads per block of the playout kernel (0: default)")
     ap.add_argument("--blocks-per-sm", type=int, default=0, help="resident blocks per SM (0: as many as fit)")
-    ap.add_argument("--workload", choices=["playouts", "searches", "serve", "learned", "train", "learned-search"],
+    ap.add_argument("--workload", choices=["playouts", "mcts", "searches", "serve", "learned", "train",
+                                           "learned-search"],
                     default="playouts")
     ap.add_argument("--net", default="", help="serve workload: network file for the learned leg")
     ap.add_argument("--positions", type=int, default=10_000_000, help="learned workload: self-play positions")
@@ -564,7 +596,8 @@ def main():
     ap.add_argument("--requests", type=int, default=2000, help="serve workload: number of requests")
     ap.add_argument("--games", type=int, default=2048, help="searches workload: number of games")
     ap.add_argument("--leaves", type=int, default=128, help="searches workload: leaves per search per step")
-    ap.add_argument("--playouts-per-leaf", type=int, default=8, help="searches workload: playouts per leaf")
+    ap.add_argument("--playouts-per-leaf", type=int, default=8, help="searches / mcts workloads: playouts per leaf")
+    ap.add_argument("--ms-per-position", type=int, default=1000, help="mcts workload: search time per position")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
@@ -572,6 +605,8 @@ def main():
         run_reference(args)
     elif args.workload == "searches":
         run_searches(args)
+    elif args.workload == "mcts":
+        run_mcts(args)
     elif args.workload == "serve":
         run_serve(args)
     elif args.workload == "learned":

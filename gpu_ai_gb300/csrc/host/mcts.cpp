@@ -31,14 +31,14 @@ double GameTree::score(int32_t n, PlayerId player) const {
 }
 
 // UCB1 weight of a child (src/mcts.cpp:182-191): untried children first.
-double GameTree::ucb1(int32_t child) const {
+// log_parent = log of the parent's finished playouts, computed once per parent.
+double GameTree::ucb1(int32_t child, double log_parent) const {
   const Node &nd = nodes_[child];
   if (nd.total == 0) return std::numeric_limits<double>::infinity();
-  const Node &par = nodes_[nd.parent];
   if (perspective_ == Perspective::ChildToMove)  // the reference's expression, long double included
-    return (double)nd.wins[nd.state.turn()] / nd.total + std::sqrt(2.0L * std::log(par.total) / nd.total);
-  const PlayerId who = par.state.turn();
-  return (double)nd.wins[who] / nd.total + c_ * std::sqrt(std::log((double)par.total) / nd.total);
+    return (double)nd.wins[nd.state.turn()] / nd.total + std::sqrt(2.0L * log_parent / nd.total);
+  const PlayerId who = nodes_[nd.parent].state.turn();
+  return (double)nd.wins[who] / nd.total + c_ * std::sqrt(log_parent / nd.total);
 }
 
 Move GameTree::getOptMove(PlayerId player) const {
@@ -138,15 +138,20 @@ void GameTree::select_rec(int32_t n, unsigned trials, std::vector<State> &out) {
   }
   const int32_t first = nodes_[n].first_child;
   const uint32_t nc = nodes_[n].nchildren;
-  std::vector<double> w(nc);
-  std::vector<unsigned> give(nc, 0);
-  std::vector<char> extra(nc, 0);
+  // per-child weights and shares; a position has at most 64 legal moves
+  double w[64];
+  unsigned give[64];
+  bool extra[64];
+  if (nc > 64) throw std::logic_error("select: more than 64 children");
   double wsum = 0;
   unsigned untried = 0;
+  const double log_parent = nodes_[n].total ? std::log((double)nodes_[n].total) : 0.0;
   for (uint32_t i = 0; i < nc; i++) {
-    w[i] = ucb1(first + (int32_t)i);
+    w[i] = ucb1(first + (int32_t)i, log_parent);
     wsum += w[i];
     if (nodes_[first + (int32_t)i].total == 0) untried++;
+    give[i] = 0;
+    extra[i] = false;
   }
   // All weights zero (a parent with one finished playout whose children have
   // not won yet, e.g. a forced move): the proportional split below would be
@@ -171,7 +176,7 @@ void GameTree::select_rec(int32_t n, unsigned trials, std::vector<State> &out) {
         opt = (int)i;
       }
     if (opt < 0) throw std::logic_error("select: cannot place the remaining trials");
-    extra[opt] = 1;
+    extra[opt] = true;
     give[opt]++;
     assigned++;
   }
@@ -182,24 +187,38 @@ void GameTree::select_rec(int32_t n, unsigned trials, std::vector<State> &out) {
 void GameTree::update(const std::vector<PlayerId> &results, unsigned playoutsPerLeaf) {
   if (results.size() != (size_t)nodes_[0].assigned * playoutsPerLeaf)
     throw std::invalid_argument("update: result count does not match the last select");
-  update_rec(0, results, 0, playoutsPerLeaf);
+  size_t at = 0;
+  update_rec(0, results, at, playoutsPerLeaf);
 }
 
-size_t GameTree::update_rec(int32_t n, const std::vector<PlayerId> &results, size_t at, unsigned k) {
+// Adds the outcomes of node n's slots (results[at ...], k per slot, in the
+// depth-first order of select) to n and its subtree; returns the wins of
+// PLAYER_1 and PLAYER_2 among them and advances `at`.  A leaf's results are
+// counted once; inner nodes add their children's counts.
+GameTree::Wins GameTree::update_rec(int32_t n, const std::vector<PlayerId> &results, size_t &at, unsigned k) {
   Node &nd = nodes_[n];
-  const size_t cnt = (size_t)nd.assigned * k;
-  nd.total += (unsigned)cnt;
-  for (size_t q = at; q < at + cnt; q++)
-    if (results[q] != PLAYER_NONE) nd.wins[results[q]]++;
+  const unsigned cnt = nd.assigned * k;
+  Wins w{0, 0};
   if (nd.expanded && !nd.terminal) {
-    size_t pos = at;
-    for (uint32_t i = 0; i < nodes_[n].nchildren; i++) {
-      const int32_t c = nodes_[n].first_child + (int32_t)i;
-      if (nodes_[c].assigned) pos = update_rec(c, results, pos, k);
+    for (uint32_t i = 0; i < nd.nchildren; i++) {
+      const int32_t c = nd.first_child + (int32_t)i;
+      if (nodes_[c].assigned) {
+        const Wins cw = update_rec(c, results, at, k);
+        w.w[0] += cw.w[0];
+        w.w[1] += cw.w[1];
+      }
     }
+  } else {
+    for (size_t q = at; q < at + cnt; q++)
+      if (results[q] != PLAYER_NONE) w.w[results[q]]++;
+    at += cnt;
   }
-  nodes_[n].assigned = 0;
-  return at + cnt;
+  Node &me = nodes_[n];  // nodes_ does not grow here, but keep the reference fresh after recursion
+  me.total += cnt;
+  me.wins[0] += w.w[0];
+  me.wins[1] += w.w[1];
+  me.assigned = 0;
+  return w;
 }
 
 }  // namespace gpuai

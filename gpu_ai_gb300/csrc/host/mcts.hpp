@@ -71,9 +71,10 @@ class GameTree {
 
   int32_t add_node(const State &s, const Move &in, int32_t parent);
   double score(int32_t n, PlayerId player) const;
-  double ucb1(int32_t child) const;
+  struct Wins { unsigned w[2]; };
+  double ucb1(int32_t child, double log_parent) const;
   void select_rec(int32_t n, unsigned trials, std::vector<State> &out);
-  size_t update_rec(int32_t n, const std::vector<PlayerId> &results, size_t at, unsigned k);
+  Wins update_rec(int32_t n, const std::vector<PlayerId> &results, size_t &at, unsigned k);
 };
 
 }  // namespace gpuai

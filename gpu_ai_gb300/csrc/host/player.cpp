@@ -83,15 +83,8 @@ void MCTSPlayer::worker() {
     lock.unlock();
     std::vector<PlayerId> results;
     try {
-      if (cfg_.playoutsPerLeaf == 1) {
-        results = driver_->runPlayouts(leaves);
-      } else {
-        std::vector<State> all;
-        all.reserve(leaves.size() * cfg_.playoutsPerLeaf);
-        for (const State &s : leaves)
-          for (unsigned k = 0; k < cfg_.playoutsPerLeaf; k++) all.push_back(s);
-        results = driver_->runPlayouts(all);
-      }
+      results = cfg_.playoutsPerLeaf == 1 ? driver_->runPlayouts(leaves)
+                                          : driver_->runPlayoutsRepeated(leaves, cfg_.playoutsPerLeaf);
     } catch (const std::exception &e) {
       lock.lock();
       error_ = e.what();

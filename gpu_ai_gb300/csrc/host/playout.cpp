@@ -46,6 +46,22 @@ std::vector<PlayerId> DevicePlayoutDriver::runPlayouts(std::vector<State> states
   return out;
 }
 
+std::vector<PlayerId> PlayoutDriver::runPlayoutsRepeated(const std::vector<State> &states, unsigned k) {
+  if (k == 1) return runPlayouts(states);
+  std::vector<State> all;
+  all.reserve(states.size() * k);
+  for (const State &s : states)
+    for (unsigned q = 0; q < k; q++) all.push_back(s);
+  return runPlayouts(std::move(all));
+}
+
+std::vector<PlayerId> DevicePlayoutDriver::runPlayoutsRepeated(const std::vector<State> &states, unsigned k) {
+  const std::vector<int8_t> r = runRepeated(states, std::vector<uint32_t>(states.size(), k));
+  std::vector<PlayerId> out(r.size());
+  for (size_t i = 0; i < r.size(); i++) out[i] = r[i] > 0 ? PLAYER_1 : (r[i] < 0 ? PLAYER_2 : PLAYER_NONE);
+  return out;
+}
+
 std::unique_ptr<PlayoutDriver> getPlayoutDriver(const std::string &name, int device, uint64_t seed) {
   if (name == "device" || name == "device_single" || name == "device_multiple" || name == "device_coarse")
     return std::make_unique<DevicePlayoutDriver>(name, GPUAI_POLICY_RANDOM, device, seed);

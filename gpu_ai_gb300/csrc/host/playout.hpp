@@ -20,6 +20,9 @@ class PlayoutDriver {
   virtual ~PlayoutDriver() {}
   virtual std::vector<PlayerId> runPlayouts(std::vector<State>) = 0;
   virtual std::string getName() const = 0;
+  // k playouts of every state, results grouped by state (k consecutive per
+  // state).  The default replicates the states for runPlayouts.
+  virtual std::vector<PlayerId> runPlayoutsRepeated(const std::vector<State> &states, unsigned k);
 };
 
 // One libgpuai context (its own CUDA stream) per driver.  Identical
@@ -34,6 +37,8 @@ class DevicePlayoutDriver : public PlayoutDriver {
   DevicePlayoutDriver &operator=(const DevicePlayoutDriver &) = delete;
 
   std::vector<PlayerId> runPlayouts(std::vector<State> states) override;
+  // One call with a repetition count of k for every state (no replication).
+  std::vector<PlayerId> runPlayoutsRepeated(const std::vector<State> &states, unsigned k) override;
   // Playouts from already-collapsed positions: reps[i] playouts of states[i].
   std::vector<int8_t> runRepeated(const std::vector<State> &states, const std::vector<uint32_t> &reps);
   std::string getName() const override { return name_; }

@@ -5,15 +5,21 @@
 //   run_ai -m playout_test -n N -1 D1 -2 D2  two playout drivers on the same states
 //   run_ai -m game_test -n G -1 P1 -2 P2     G games between two players
 //   run_ai -m game -1 P1 -2 P2               one game, printed
+//   run_ai -m mcts_bench -n N -1 D1 -2 D2    host UCT searches from N positions with
+//                                            GPU leaf batches, per playout driver
 //
 // Extra options: --seed S (positions and random streams), --ms-per-move T
-// (MCTS move time), --device D.
+// (MCTS move time), --device D; for mcts_bench --leaves-min/--leaves-max L
+// (leaf slots per batch), --playouts-per-leaf P and --threads T (searches run
+// concurrently, one playout driver and CUDA stream each).
+#include <atomic>
 #include <chrono>
 #include <cstdlib>
 #include <cstring>
 #include <iostream>
 #include <stdexcept>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "host/mcts.hpp"
@@ -33,11 +39,14 @@ struct Options {
   uint64_t seed = 2016;
   unsigned ms_per_move = 1000;
   int device = 0;
+  unsigned leaves_min = 16384, leaves_max = 65536, playouts_per_leaf = 4;
+  unsigned threads = 0;  // mcts_bench: concurrent searches (0: min(16, hardware threads))
 };
 
 void usage(std::ostream &os) {
-  os << "usage: run_ai -m {gen_moves_test,playout_test,game_test,game} [-n N] [-1 X] [-2 Y]\n"
+  os << "usage: run_ai -m {gen_moves_test,playout_test,game_test,game,mcts_bench} [-n N] [-1 X] [-2 Y]\n"
         "              [--seed S] [--ms-per-move T] [--device D]\n"
+        "              [--leaves-min L] [--leaves-max L] [--playouts-per-leaf P] [--threads T]\n"
         "  playout drivers: device device_single device_multiple device_coarse device_heuristic\n"
         "                   device_eps_greedy\n"
         "  players: random mcts mcts_device_single mcts_device_multiple mcts_device_coarse\n"
@@ -60,10 +69,17 @@ Options parse(int argc, char **argv) {
     else if (a == "--seed") o.seed = std::stoull(val());
     else if (a == "--ms-per-move") o.ms_per_move = (unsigned)std::stoul(val());
     else if (a == "--device") o.device = std::stoi(val());
+    else if (a == "--leaves-min") o.leaves_min = (unsigned)std::stoul(val());
+    else if (a == "--leaves-max") o.leaves_max = (unsigned)std::stoul(val());
+    else if (a == "--playouts-per-leaf") o.playouts_per_leaf = (unsigned)std::stoul(val());
+    else if (a == "--threads") o.threads = (unsigned)std::stoul(val());
     else throw std::invalid_argument("unknown option " + a);
   }
-  if (o.mode != "gen_moves_test" && o.mode != "playout_test" && o.mode != "game_test" && o.mode != "game")
+  if (o.mode != "gen_moves_test" && o.mode != "playout_test" && o.mode != "game_test" && o.mode != "game" &&
+      o.mode != "mcts_bench")
     throw std::invalid_argument("Unknown run mode");
+  if (o.leaves_min == 0 || o.leaves_max < o.leaves_min || o.playouts_per_leaf == 0)
+    throw std::invalid_argument("need 0 < leaves-min <= leaves-max and playouts-per-leaf > 0");
   return o;
 }
 
@@ -179,6 +195,92 @@ int game_tests(const Options &o, bool single) {
   return 0;
 }
 
+// Host UCT searches as MCTSPlayer's worker runs them (src/player.cpp:134-150):
+// select a batch of leaf slots (total trials x 0.05, clamped to
+// [leaves_min, leaves_max]), playouts_per_leaf playouts per slot through the
+// playout driver, fold the outcomes back; ms_per_move of searching per
+// position (10-40 random plies from the start, seeded).  `threads` searches
+// run at once, each thread with its own driver (context and CUDA stream), as
+// the reference runs one worker thread per MCTSPlayer.  One JSON line per
+// driver name: playouts/s over the wall time, and the share of the searching
+// threads' time spent inside the driver calls.
+int mcts_bench(const Options &o) {
+  const unsigned n = o.n_set ? o.n : 32;
+  unsigned threads = o.threads;
+  if (threads == 0) {
+    const unsigned hw = std::thread::hardware_concurrency();
+    threads = hw == 0 ? 1 : (hw < 16 ? hw : 16);
+  }
+  if (threads > n) threads = n;
+  const std::vector<State> roots = genRandomStates(n, o.seed, 10, 40);
+  std::vector<std::string> names;
+  names.push_back(o.p1.empty() ? "device" : o.p1);
+  if (!o.p2.empty()) names.push_back(o.p2);
+  for (const std::string &name : names) {
+    std::vector<std::unique_ptr<PlayoutDriver>> drivers;
+    for (unsigned t = 0; t < threads; t++) {
+      drivers.push_back(getPlayoutDriver(name, o.device, o.seed + 1000003ull * t));
+      drivers.back()->runPlayouts(std::vector<State>(roots.begin(), roots.end()));  // warm up
+    }
+    struct Acc { uint64_t playouts = 0, batches = 0, leaves = 0, searched = 0; double driver_s = 0, search_s = 0; };
+    std::vector<Acc> acc(threads);
+    std::atomic<unsigned> next{0};
+    std::vector<std::string> errors(threads);
+    const auto w0 = std::chrono::steady_clock::now();
+    std::vector<std::thread> pool;
+    for (unsigned t = 0; t < threads; t++) {
+      pool.emplace_back([&, t] {
+        try {
+          Acc &a = acc[t];
+          for (unsigned i; (i = next.fetch_add(1)) < n;) {
+            if (roots[i].isGameOver()) continue;
+            a.searched++;
+            GameTree tree(roots[i]);
+            const auto t0 = std::chrono::steady_clock::now();
+            const auto until = t0 + std::chrono::milliseconds(o.ms_per_move);
+            while (std::chrono::steady_clock::now() < until) {
+              unsigned k = (unsigned)(tree.getTotalTrials() * 0.05);
+              k = k < o.leaves_min ? o.leaves_min : (k > o.leaves_max ? o.leaves_max : k);
+              const std::vector<State> slots = tree.select(k);
+              const auto c0 = std::chrono::steady_clock::now();
+              const std::vector<PlayerId> r = drivers[t]->runPlayoutsRepeated(slots, o.playouts_per_leaf);
+              a.driver_s += std::chrono::duration<double>(std::chrono::steady_clock::now() - c0).count();
+              tree.update(r, o.playouts_per_leaf);
+              a.playouts += r.size();
+              a.leaves += slots.size();
+              a.batches++;
+            }
+            a.search_s += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+          }
+        } catch (const std::exception &e) {
+          errors[t] = e.what();
+        }
+      });
+    }
+    for (std::thread &th : pool) th.join();
+    const double wall = std::chrono::duration<double>(std::chrono::steady_clock::now() - w0).count();
+    for (const std::string &e : errors)
+      if (!e.empty()) throw std::runtime_error(e);
+    Acc tot;
+    for (const Acc &a : acc) {
+      tot.playouts += a.playouts; tot.batches += a.batches; tot.leaves += a.leaves; tot.searched += a.searched;
+      tot.driver_s += a.driver_s; tot.search_s += a.search_s;
+    }
+    std::cout << "MCTS_BENCH {\"driver\": \"" << name << "\", \"positions\": " << tot.searched
+              << ", \"threads\": " << threads << ", \"ms_per_position\": " << o.ms_per_move
+              << ", \"playouts\": " << tot.playouts << ", \"batches\": " << tot.batches
+              << ", \"leaves\": " << tot.leaves << ", \"mean_leaves_per_batch\": "
+              << (tot.batches ? (double)tot.leaves / tot.batches : 0.0)
+              << ", \"playouts_per_leaf\": " << o.playouts_per_leaf << ", \"seconds\": " << wall
+              << ", \"playouts_per_s\": " << (wall > 0 ? tot.playouts / wall : 0.0)
+              << ", \"search_seconds\": " << tot.search_s << ", \"driver_seconds\": " << tot.driver_s
+              << ", \"driver_share\": " << (tot.search_s > 0 ? tot.driver_s / tot.search_s : 0.0)
+              << ", \"mean_driver_call_ms\": " << (tot.batches ? 1e3 * tot.driver_s / tot.batches : 0.0) << "}"
+              << std::endl;
+  }
+  return 0;
+}
+
 }  // namespace
 
 int main(int argc, char **argv) {
@@ -194,6 +296,7 @@ int main(int argc, char **argv) {
     if (o.mode == "gen_moves_test") return gen_moves_tests(o);
     if (o.mode == "playout_test") return playout_tests(o);
     if (o.mode == "game_test") return game_tests(o, false);
+    if (o.mode == "mcts_bench") return mcts_bench(o);
     return game_tests(o, true);
   } catch (const std::exception &e) {
     std::cerr << "error: " << e.what() << std::endl;

@@ -47,3 +47,19 @@ def test_mcts_beats_random(lib_built):
     assert rc == 0, out
     p1, d, p2 = counts(out)[-1]
     assert p1 + d + p2 == 2 and p2 == 0 and p1 >= 1
+
+
+def test_mcts_bench_reports_leaf_batch_throughput(lib_built):
+    """mcts_bench: host UCT searches with GPU leaf batches of 16K+ slots run for
+    the requested time and account for every playout."""
+    import json
+    rc, out = run("-m", "mcts_bench", "-n", "3", "--ms-per-move", "60", "--playouts-per-leaf", "2",
+                  "--threads", "2", "-1", "device", "-2", "device_eps_greedy")
+    assert rc == 0, out
+    lines = [json.loads(x[len("MCTS_BENCH "):]) for x in out.splitlines() if x.startswith("MCTS_BENCH ")]
+    assert [x["driver"] for x in lines] == ["device", "device_eps_greedy"]
+    for x in lines:
+        assert x["positions"] == 3 and x["batches"] >= 3 and x["threads"] == 2
+        assert x["mean_leaves_per_batch"] >= 16384
+        assert x["playouts"] == 2 * x["leaves"]
+        assert 0 < x["driver_seconds"] <= x["search_seconds"] <= 2 * x["seconds"]
