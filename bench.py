@@ -38,6 +38,7 @@ METRIC = "checkers playouts/sec on 1 GB300 vs host CPU; win rate vs plain at equ
 UNIT = "playouts/s"
 N_POS, REPS, POS_SEED, MAX_PLIES = 64, 4096, 2016, 30
 TOTAL = N_POS * REPS
+REPS_BENCH = REPS
 WORKLOAD = {
     "workload": "uniform random playouts: 64 seeded positions (0-30 random plies, seed 2016) x 4096",
     "positions": N_POS,
@@ -52,7 +53,7 @@ WORKLOAD = {
 OPS_PER_PLY = 260.0
 # DRAM bytes per launch of the playout kernel from one ncu capture
 # (dram__bytes_read.sum + dram__bytes_write.sum).
-TRAFFIC_BYTES = 39424  # one ncu capture of the benchmark launch: 39.4 KB read, 0 B written
+TRAFFIC_BYTES = 44032  # one ncu capture of the benchmark launch: 44.0 KB read, 0 B written
 
 
 def measured_peaks():
@@ -213,7 +214,17 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def workload(reps):
+    """The playouts workload with `reps` playouts per position (4,096 is the
+    benchmark batch)."""
+    w = dict(WORKLOAD, playouts_per_position=reps, playouts_per_step=N_POS * reps)
+    if reps != REPS:
+        w["workload"] = (f"uniform random playouts: 64 seeded positions (0-30 random plies, seed 2016) x {reps}")
+    return w
+
+
 def run_ours(args):
+    REPS, TOTAL = args.playouts_per_position, N_POS * args.playouts_per_position  # noqa: N806
     rank, world, local = dist_setup(args.gpus)
     import torch
     from gpu_ai_gb300 import Engine
@@ -299,7 +310,8 @@ def run_ours(args):
     plies_s = plies / kern_s
     roof = {"bound": "int_issue", "unit": "Tlane-op/s",
             "peak": peak_ops / 1e12, "peak_source": f"{info['sms']} SMs x 128 lanes x {sm_mhz:.0f} MHz ({src})",
-            "ops_per_ply": OPS_PER_PLY, "plies_per_s": plies_s, "traffic": TRAFFIC_BYTES}
+            "ops_per_ply": OPS_PER_PLY, "plies_per_s": plies_s,
+            "traffic": TRAFFIC_BYTES if REPS == REPS_BENCH else None}
     if OPS_PER_PLY:
         roof["achieved"] = plies_s * OPS_PER_PLY / 1e12
         roof["frac"] = roof["achieved"] / roof["peak"]
@@ -312,7 +324,7 @@ def run_ours(args):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": kern_s / args.steps * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic (seeded positions)",
-        "config": dict(WORKLOAD, parallelism=f"replicas{world}" if world > 1 else "single"),
+        "config": dict(workload(REPS), parallelism=f"replicas{world}" if world > 1 else "single"),
         "plies_per_playout": plies / (args.steps * TOTAL),
         "wall_ms_per_step": wall / args.steps * 1e3,
         "gpu_launches": args.steps,
@@ -581,6 +593,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--playouts-per-position", type=int, default=REPS,
+                    help="playouts workload: playouts per position (4,096 is the benchmark batch)")
     ap.add_argument("--block", type=int, default=0, help="threads per block of the playout kernel (0: default)")
     ap.add_argument("--blocks-per-sm", type=int, default=0, help="resident blocks per SM (0: as many as fit)")
     ap.add_argument("--workload", choices=["playouts", "mcts", "searches", "serve", "learned", "train",
