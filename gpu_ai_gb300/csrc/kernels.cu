@@ -93,10 +93,12 @@ __global__ void __launch_bounds__(BLOCK) playout_kernel(PlayoutArgs a) {
   uint32_t j = 0, plies_here = 0, game_plies = 0;
   bool have = false, exhausted = false;
 
-  if constexpr (POLICY == 0) {
+  if constexpr (POLICY == 0 || POLICY == 2) {
     // Uniform random policy: at most one draw per ply, so Philox blocks are
     // generated for the whole warp every fourth iteration (DrawRing keeps four
     // or more draws buffered) and new games start on those iterations too.
+    // eps-greedy (policy 2, play_ply_eps_sched) takes at most two draws per
+    // ply and refills every second iteration.
     // Plies whose capture can be extended take longer code: men's multi-jumps
     // (about 2.6% of plies) are deferred to every kMenPeriod-th iteration and
     // plies where a king's capture can continue (about 0.7%, the costlier
@@ -124,8 +126,9 @@ __global__ void __launch_bounds__(BLOCK) playout_kernel(PlayoutArgs a) {
     uint32_t pend = 0;    // deferred ply: 0 none, 1 men's multi-jump, 2 king capture search
     bool sparse = false;  // warp-uniform: the work ran out and the warp holds kSparseLanes games or fewer
     auto pick = [&](uint32_t n) { return rs.pick(n); };
+    constexpr uint32_t kRefillMask = POLICY == 2 ? 1u : 3u;
     for (uint32_t it = 0;; ++it) {
-      if ((it & 3u) == 0) {
+      if ((it & kRefillMask) == 0) {
         if (claim(a, have, j, exhausted, lane)) {
           have = true;
           const uint32_t p = position_of(a, j);
@@ -145,7 +148,9 @@ __global__ void __launch_bounds__(BLOCK) playout_kernel(PlayoutArgs a) {
           have = false;
           break;
         }
-        const int n = play_ply_sched(b, pick, men_ok, king_ok);
+        int n;
+        if constexpr (POLICY == 2) n = play_ply_eps_sched(b, rs, men_ok, king_ok);
+        else n = play_ply_sched(b, pick, men_ok, king_ok);
         if (n == kNeedMen || n == kNeedKing) {
           pend = n == kNeedMen ? 1u : 2u;
           break;

@@ -900,6 +900,136 @@ GA_HD int ply_eps_greedy(Board &b, Rng &rs) {
   return n;
 }
 
+// ------------------------------------------------------------ eps-greedy without enumeration
+
+// Bit plane q of a per-square value c + sgn * row (4 squares per row).
+constexpr uint32_t row_value_plane(int q, int c, int sgn) {
+  uint32_t m = 0;
+  for (int r = 0; r < 8; r++)
+    if (((c + sgn * r) >> q) & 1) m |= 0xFu << (4 * r);
+  return m;
+}
+
+// eps_delta + 1 of a single jump by a man that does not promote, minus 3,
+// for a captured man, by the jumping square's row: 4 + the captured man's
+// advancement.  PLAYER_1 moving up (captured man one row above): 10 - row;
+// down: 12 - row; PLAYER_2 up: 5 + row; down: 3 + row.  Four bit planes each.
+struct RowValue { uint32_t q0, q1, q2, q3; };
+constexpr RowValue row_value(int c, int sgn) {
+  return RowValue{row_value_plane(0, c, sgn), row_value_plane(1, c, sgn), row_value_plane(2, c, sgn),
+                  row_value_plane(3, c, sgn)};
+}
+
+// The moves of largest eps_delta among the moves M[0..3] of a position where
+// no capture can continue, as subsets B[0..3] (list order is kept, so move i
+// of B is the i-th best move of the list).  Direct moves: a man's step +1, a
+// king's 0, a promoting step -2.  Single jumps: captured king 8, captured man
+// 4 + its advancement; a man's jump +2, a promoting jump -1, a king's 0.
+// The jump values (+1, at most 13) are kept as four bit planes per direction
+// and the maximum is found bit by bit from the top plane.
+template <int D>
+GA_HD void eps_jump_planes(const Side &s, uint32_t m, uint32_t oppK, uint32_t men, uint32_t promoJ, uint32_t y[4]) {
+  constexpr bool up = D < 2;
+  constexpr RowValue p1 = up ? row_value(10, -1) : row_value(12, -1);
+  constexpr RowValue p2 = up ? row_value(5, 1) : row_value(3, 1);
+  const uint32_t w0 = s.turn ? p2.q0 : p1.q0, w1 = s.turn ? p2.q1 : p1.q1;
+  const uint32_t w2 = s.turn ? p2.q2 : p1.q2, w3 = s.turn ? p2.q3 : p1.q3;
+  const uint32_t ck = m & step<3 - D>(oppK);  // the jumped square holds a king: value 8
+  const uint32_t x0 = w0 & ~ck, x1 = w1 & ~ck, x2 = w2 & ~ck, x3 = w3 | ck;
+  const uint32_t mnp = m & men & ~promoJ;
+  const uint32_t a0 = (m & s.ownK) | mnp, a1 = mnp;  // + 1 for a king, + 3 for a man, + 0 for a promoting man
+  const uint32_t c0 = x0 & a0;
+  const uint32_t c1 = (x1 & a1) | (c0 & (x1 ^ a1));
+  const uint32_t c2 = x2 & c1;
+  y[0] = x0 ^ a0;
+  y[1] = x1 ^ a1 ^ c0;
+  y[2] = x2 ^ c1;
+  y[3] = x3 ^ c2;
+}
+
+GA_HD void eps_best(const Board &b, const Side &s, bool capture, const uint32_t M[4], uint32_t B[4]) {
+  const uint32_t men = s.own & ~s.ownK;
+  if (!capture) {
+    const uint32_t promoD = s.turn ? 0x000000F0u : 0x0F000000u;  // a man stepping from here promotes
+    uint32_t np = 0, kk = 0;
+GA_UNROLL
+    for (int d = 0; d < 4; d++) {
+      np |= M[d] & men & ~promoD;
+      kk |= M[d] & s.ownK;
+    }
+GA_UNROLL
+    for (int d = 0; d < 4; d++)
+      B[d] = np ? (M[d] & men & ~promoD) : (kk ? (M[d] & s.ownK) : (M[d] & men & promoD));
+    return;
+  }
+  const uint32_t oppK = s.opp & b.kings;
+  const uint32_t promoJ = s.turn ? 0x00000F00u : 0x00F00000u;  // a man jumping from here promotes
+  uint32_t y0[4], y1[4], y2[4], y3[4];
+  eps_jump_planes<0>(s, M[0], oppK, men, promoJ, y0);
+  eps_jump_planes<1>(s, M[1], oppK, men, promoJ, y1);
+  eps_jump_planes<2>(s, M[2], oppK, men, promoJ, y2);
+  eps_jump_planes<3>(s, M[3], oppK, men, promoJ, y3);
+  uint32_t c0 = M[0], c1 = M[1], c2 = M[2], c3 = M[3];
+GA_UNROLL
+  for (int q = 3; q >= 0; q--) {
+    const uint32_t t0 = c0 & y0[q], t1 = c1 & y1[q], t2 = c2 & y2[q], t3 = c3 & y3[q];
+    const bool any = (t0 | t1 | t2 | t3) != 0;
+    c0 = any ? t0 : c0;
+    c1 = any ? t1 : c1;
+    c2 = any ? t2 : c2;
+    c3 = any ? t3 : c3;
+  }
+  B[0] = c0; B[1] = c1; B[2] = c2; B[3] = c3;
+}
+
+// One eps-greedy ply (the move ply_eps_greedy plays, with the same draws):
+// branch-free for direct moves and captures that cannot continue; the rarer
+// plies are deferred as in play_ply_sched (kNeedMen / kNeedKing) or played by
+// ply_eps_greedy's enumeration.
+template <class Rng>
+GA_HD int play_ply_eps_sched(Board &b, Rng &rs, bool men_now, bool king_now) {
+  Side s;
+  make_side(b, s);
+  const uint32_t men = s.own & ~s.ownK;
+  const uint32_t m01 = s.turn ? s.ownK : s.own;
+  const uint32_t m23 = s.turn ? s.own : s.ownK;
+  const uint32_t J0 = m01 & s.jd[0], J1 = m01 & s.jd[1], J2 = m23 & s.jd[2], J3 = m23 & s.jd[3];
+  const bool capture = (J0 | J1 | J2 | J3) != 0;
+  const uint32_t jall = s.jd[0] | s.jd[1] | s.jd[2] | s.jd[3];
+  const uint32_t jf = s.turn ? (s.jd[2] | s.jd[3]) : (s.jd[0] | s.jd[1]);
+  const uint32_t lm = jump2<0>(J0 & men) | jump2<1>(J1 & men) | jump2<2>(J2 & men) | jump2<3>(J3 & men);
+  const uint32_t lk = jump2<0>(J0 & s.ownK) | jump2<1>(J1 & s.ownK) | jump2<2>(J2 & s.ownK) |
+                      jump2<3>(J3 & s.ownK);
+  const uint32_t cont_k = lk & jall, cont_m = lm & jf;
+  if (cont_k | cont_m) {
+    if (cont_k && !king_now) return kNeedKing;
+    if (!cont_k && !men_now) return kNeedMen;
+    return ply_eps_greedy(b, rs);
+  }
+  const uint32_t M[4] = {capture ? J0 : (m01 & step<3>(s.empty)), capture ? J1 : (m01 & step<2>(s.empty)),
+                         capture ? J2 : (m23 & step<1>(s.empty)), capture ? J3 : (m23 & step<0>(s.empty))};
+  const int n = popc(M[0]) + popc(M[1]) + popc(M[2]) + popc(M[3]);
+  if (n == 0) return 0;
+  uint32_t B[4];
+  eps_best(b, s, capture, M, B);
+  uint32_t S0 = M[0], S1 = M[1], S2 = M[2], S3 = M[3], idx = 0;
+  if (n >= 2) {
+    const bool uniform = rs.next() < kEpsThreshold;
+    const uint32_t ties = (uint32_t)(popc(B[0]) + popc(B[1]) + popc(B[2]) + popc(B[3]));
+    const uint32_t cnt = uniform ? (uint32_t)n : ties;
+    S0 = uniform ? S0 : B[0];
+    S1 = uniform ? S1 : B[1];
+    S2 = uniform ? S2 : B[2];
+    S3 = uniform ? S3 : B[3];
+    if (cnt >= 2) idx = mulhi_index(rs.next(), cnt);
+  }
+  int from, to;
+  uint32_t removed;
+  nth_move(S0, S1, S2, S3, idx, capture, men, from, to, removed);
+  apply_move(b, from, to, removed);
+  return n;
+}
+
 template <int POLICY, class Rng>
 GA_HD int ply(Board &b, Rng &rs) {
   if (POLICY == 1) return ply_ref_heuristic(b, rs);

@@ -64,13 +64,14 @@ int rh_playout(const uint32_t *pos, uint64_t seed, uint64_t id, int policy, uint
   return outcome;
 }
 
-// The same playout with the uniform-random kernel's schedule: Philox blocks
-// generated every fourth iteration (DrawRing), men's multi-jumps and king
+// The same playout with the warp loop's schedule (uniform random policy 0 or
+// eps-greedy policy 2): Philox blocks generated every fourth (every second
+// for eps-greedy) iteration (DrawRing), men's multi-jumps and king
 // capture searches deferred to their own iterations, as the warp loop does;
 // from iteration sparse_from on nothing is deferred (the kernel's schedule for
 // a warp left with few games).
-int rh_playout_ring(const uint32_t *pos, uint64_t seed, uint64_t id, uint32_t sparse_from, uint32_t *plies,
-                    uint32_t *draws) {
+int rh_playout_ring(const uint32_t *pos, uint64_t seed, uint64_t id, uint32_t sparse_from, int policy,
+                    uint32_t *plies, uint32_t *draws) {
   Board b = load(pos);
   DrawRing rs;
   rs.start(seed, id, 0);
@@ -79,13 +80,13 @@ int rh_playout_ring(const uint32_t *pos, uint64_t seed, uint64_t id, uint32_t sp
   int outcome = 0;
   uint32_t pend = 0;
   for (uint32_t it = 0;; ++it) {
-    if ((it & 3u) == 0) rs.refill();
+    if ((it & (policy == 2 ? 1u : 3u)) == 0) rs.refill();  // eps-greedy takes up to two draws per ply
     const bool sparse = it >= sparse_from;
     const bool men_ok = sparse || (it & (kMenPeriod - 1u)) == kMenPhase;
     const bool king_ok = sparse || (it & (kKingPeriod - 1u)) == kKingPhase;
     if ((pend == 1u && !men_ok) || (pend == 2u && !king_ok)) continue;
     if (((b.meta >> 8) & 0xffu) >= (uint32_t)kDrawPlies) { outcome = 0; break; }
-    const int n = play_ply_sched(b, pick, men_ok, king_ok);
+    const int n = policy == 2 ? play_ply_eps_sched(b, rs, men_ok, king_ok) : play_ply_sched(b, pick, men_ok, king_ok);
     if (n == kNeedMen || n == kNeedKing) { pend = n == kNeedMen ? 1u : 2u; continue; }
     pend = 0;
     if (n == 0) { outcome = (b.meta & 1u) ? 1 : -1; break; }

@@ -31,7 +31,7 @@ def rh():
     lib = ctypes.CDLL(SO)
     lib.rh_genmoves_b16.argtypes = [u32p, ctypes.c_uint32, u8p, ctypes.c_uint32, u8p]
     lib.rh_playout.argtypes = [u32p, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int, u32p, u32p]
-    lib.rh_playout_ring.argtypes = [u32p, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint32, u32p, u32p]
+    lib.rh_playout_ring.argtypes = [u32p, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint32, ctypes.c_int, u32p, u32p]
     lib.rh_random_positions.argtypes = [ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, u32p]
     return lib
 
@@ -80,15 +80,17 @@ def test_playouts_replay_on_oracle(rh, policy):
         assert (o, int(pl[0]), int(dr[0])) == L.replay_one(p, 77, 1000 + i, policy), (policy, i)
 
 
-def test_buffered_draw_schedule_replays_on_oracle(rh):
-    """The warp-synchronous Philox schedule of the random-policy kernel
-    consumes exactly the stream the oracle replays."""
+@pytest.mark.parametrize("policy", [0, 2])
+def test_buffered_draw_schedule_replays_on_oracle(rh, policy):
+    """The warp-synchronous Philox schedule of the random and eps-greedy
+    kernels (branch-free plies, deferred capture searches) consumes exactly the
+    stream the oracle replays."""
     pos = np.concatenate([L.random_positions(12, 500, 0, 80), crafted_boards()])
     for i in range(3000):
         p = np.ascontiguousarray(pos[i % len(pos)])
         pl = np.zeros(1, np.uint32)
         dr = np.zeros(1, np.uint32)
         sparse_from = (0, 37, 1 << 30)[i % 3]  # defers nothing from the start / from iteration 37 / never
-        o = rh.rh_playout_ring(p.ctypes.data_as(u32p), 4242, i * 7, sparse_from, pl.ctypes.data_as(u32p),
+        o = rh.rh_playout_ring(p.ctypes.data_as(u32p), 4242, i * 7, sparse_from, policy, pl.ctypes.data_as(u32p),
                                dr.ctypes.data_as(u32p))
-        assert (o, int(pl[0]), int(dr[0])) == L.replay_one(p, 4242, i * 7, 0), i
+        assert (o, int(pl[0]), int(dr[0])) == L.replay_one(p, 4242, i * 7, policy), (policy, i)
