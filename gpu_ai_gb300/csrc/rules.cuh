@@ -121,11 +121,12 @@ GA_HD void make_side(const Board &b, Side &s) {
   s.opp = s.turn ? b.p1 : b.p2;
   s.ownK = s.own & b.kings;
   s.empty = ~(b.p1 | b.p2);
-  // jd[d] = {s : s+d is an opponent, s+2d is empty}; step<3-d> is the inverse of step<d>.
-  s.jd[0] = step<3>(s.opp) & jump2_back<0>(s.empty);
-  s.jd[1] = step<2>(s.opp) & jump2_back<1>(s.empty);
-  s.jd[2] = step<1>(s.opp) & jump2_back<2>(s.empty);
-  s.jd[3] = step<0>(s.opp) & jump2_back<3>(s.empty);
+  // jd[d] = {s : s+d is an opponent, s+2d is empty}; step<3-d> is the inverse of
+  // step<d>, and step<3-d>(empty) is also the direct-move source mask of d.
+  s.jd[0] = step<3>(s.opp & step<3>(s.empty));
+  s.jd[1] = step<2>(s.opp & step<2>(s.empty));
+  s.jd[2] = step<1>(s.opp & step<1>(s.empty));
+  s.jd[3] = step<0>(s.opp & step<0>(s.empty));
 }
 
 // Pieces of the side to move that have at least one capture.
@@ -421,13 +422,6 @@ GA_HD int nth_bit4(uint32_t dm, uint32_t rem) {
   return (int)((word >> (2u * (idx & 15u))) & 3u);
 }
 
-// Byte-wise population counts: byte k of the result = popcount of byte k of x.
-GA_HD uint32_t popc8(uint32_t x) {
-  x = x - ((x >> 1) & 0x55555555u);
-  x = (x & 0x33333333u) + ((x >> 2) & 0x33333333u);
-  return (x + (x >> 4)) & 0x0F0F0F0Fu;
-}
-
 // Bits 0..3 of x spread to bits 0, 8, 16, 24 (x < 16).
 GA_HD uint32_t spread4(uint32_t x) { return (x * 0x00204081u) & 0x01010101u; }
 
@@ -443,44 +437,45 @@ GA_HD uint32_t bytes_le(uint32_t P, uint32_t i) {
 // moves in one direction each; squares ascending, within a square the
 // directions ascending, or descending for a man's captures, which search
 // dc = -1 first).  Returns the source square, the destination square and the
-// captured squares.  The square is found with byte-wise prefix sums of the
-// per-square move counts instead of a search over prefix popcounts, and the
-// direction from the prefix of the square's direction bits: a short chain of
-// full-rate integer operations.  Every square holds at most four moves and
-// the list at most 48, so every prefix sum fits a byte below 128.
-GA_HD void nth_move(uint32_t M0, uint32_t M1, uint32_t M2, uint32_t M3, uint32_t i, bool capture, uint32_t men,
-                    int &from, int &to, uint32_t &removed) {
-  // per-square move counts (0..4) as three bit planes
+// captured squares.  No search over the squares: the per-square move counts
+// (0..4) are three bit planes; the moves below squares 8, 16 and 24 are
+// counted with POPC (the XU pipe, idle in the playout kernel, whose integer
+// ALU pipe is the busy one) and three compares pick the byte; the chosen
+// byte's low half is counted the same way; the chosen half's four counts are
+// spread to bytes by one multiply and a byte-parallel compare of their prefix
+// sums picks the square; the direction is the rank among the square's
+// direction bits, found by three compares.  Every square holds at most four
+// moves, so every prefix sum of a half fits a byte below 128.
+GA_HD void nth_move(uint32_t M0, uint32_t M1, uint32_t M2, uint32_t M3, uint32_t i, bool capture,
+                         uint32_t men, int &from, int &to, uint32_t &removed) {
   const uint32_t a0 = M0 ^ M1, a1 = M0 & M1, b0 = M2 ^ M3, b1 = M2 & M3;
   const uint32_t S0 = a0 ^ b0, k0 = a0 & b0;
   const uint32_t S1 = a1 ^ b1 ^ k0, S2 = (a1 & b1) | (k0 & (a1 ^ b1));
-  // inclusive prefix sums over the four bytes (eight squares each)
-  const uint32_t P = (popc8(S0) + 2u * popc8(S1) + 4u * popc8(S2)) * 0x01010101u;
-  const uint32_t g = bytes_le(P, i);
-  const uint32_t sh = 8u * g;
-  const uint32_t rem = i - (((P << 8) >> sh) & 0xffu);
-  // the byte's two halves (four squares each): counts per square as bytes
+  // moves on squares below 8, 16, 24
+  const uint32_t P1 = (uint32_t)(popc(S0 & 0xFFu) + 2 * popc(S1 & 0xFFu) + 4 * popc(S2 & 0xFFu));
+  const uint32_t P2 = (uint32_t)(popc(S0 & 0xFFFFu) + 2 * popc(S1 & 0xFFFFu) + 4 * popc(S2 & 0xFFFFu));
+  const uint32_t P3 = (uint32_t)(popc(S0 & 0xFFFFFFu) + 2 * popc(S1 & 0xFFFFFFu) + 4 * popc(S2 & 0xFFFFFFu));
+  const bool g1 = i >= P1, g2 = i >= P2, g3 = i >= P3;
+  const uint32_t sh = g3 ? 24u : (g2 ? 16u : (g1 ? 8u : 0u));
+  const uint32_t rem = i - (g3 ? P3 : (g2 ? P2 : (g1 ? P1 : 0u)));
   const uint32_t e0 = S0 >> sh, e1 = S1 >> sh, e2 = S2 >> sh;
-  const uint32_t Qlo = spread4(e0 & 15u) + 2u * spread4(e1 & 15u) + 4u * spread4(e2 & 15u);
-  const uint32_t Qhi = spread4((e0 >> 4) & 15u) + 2u * spread4((e1 >> 4) & 15u) + 4u * spread4((e2 >> 4) & 15u);
-  const uint32_t Rlo = Qlo * 0x01010101u;
-  const uint32_t tlo = Rlo >> 24;
+  const uint32_t tlo = (uint32_t)(popc(e0 & 15u) + 2 * popc(e1 & 15u) + 4 * popc(e2 & 15u));
   const bool hi = rem >= tlo;
-  const uint32_t Q = hi ? Qhi : Qlo;
+  const uint32_t hs = hi ? 4u : 0u;
+  const uint32_t Q = spread4((e0 >> hs) & 15u) + 2u * spread4((e1 >> hs) & 15u) + 4u * spread4((e2 >> hs) & 15u);
   const uint32_t R = Q * 0x01010101u;
   const uint32_t rem2 = hi ? rem - tlo : rem;
   const uint32_t q = bytes_le(R, rem2);
-  const uint32_t sq = sh + (hi ? 4u : 0u) + q;
-  const uint32_t r0 = rem2 - (((R << 8) >> (8u * q)) & 0xffu);  // rank among the square's moves
+  const uint32_t sq = sh + hs + q;
+  const uint32_t r0 = rem2 - (((R << 8) >> (8u * q)) & 0xffu);
   const uint32_t cnt = (Q >> (8u * q)) & 0xffu;
   const uint32_t x0 = (M0 >> sq) & 1u, x1 = (M1 >> sq) & 1u, x2 = (M2 >> sq) & 1u;
   const uint32_t r = (capture && ((men >> sq) & 1u)) ? cnt - 1u - r0 : r0;
   const uint32_t c01 = x0 + x1;
-  // direction = the r-th set bit of (x0, x1, x2, x3)
   const uint32_t d = (uint32_t)(r >= x0) + (uint32_t)(r >= c01) + (uint32_t)(r >= c01 + x2);
   const uint32_t sd = 8u * d;
   const int s = (int)sq;
-  const int mid = s + (int)((0x00010809u >> sd) & 0xffu) - 5 + (((s >> 2) & 1) ^ 1);  // one step along d
+  const int mid = s + (int)((0x00010809u >> sd) & 0xffu) - 5 + (((s >> 2) & 1) ^ 1);
   from = s;
   to = capture ? s + (int)((0x00021012u >> sd) & 0xffu) - 9 : mid;
   removed = capture ? 1u << mid : 0u;

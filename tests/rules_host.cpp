@@ -114,3 +114,35 @@ void rh_random_positions(uint64_t seed, uint32_t n, uint32_t min_plies, uint32_t
 }
 
 }  // extern "C"
+
+extern "C" {
+// Branch-free eps-greedy ply (play_ply_eps_sched) against the enumerating
+// ply_eps_greedy on n pseudo-random boards (any occupancy, kings included,
+// seeded splitmix64): same move count, same board after the ply, same draws.
+// Returns the number of boards that differ.
+long rh_eps_fast_matches_enum(uint64_t n, uint64_t seed) {
+  uint64_t x = seed;
+  auto next = [&]() {
+    uint64_t z = (x += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+  };
+  long bad = 0;
+  for (uint64_t t = 0; t < n; t++) {
+    uint32_t occ = (uint32_t)next() & (uint32_t)next();
+    if (t & 1) occ |= (uint32_t)next() & (uint32_t)next();
+    const uint32_t side = (uint32_t)next();
+    const uint32_t kmask = t % 3 == 0 ? (uint32_t)next() : (t % 3 == 1 ? 0u : ~0u);
+    const Board b0 = {occ & side, occ & ~side, occ & kmask, (uint32_t)(next() & 1)};
+    Board a = b0, c = b0;
+    Stream ra, rc;
+    ra.init(seed, t, 0);
+    rc.init(seed, t, 0);
+    const int na = ply_eps_greedy(a, ra);
+    const int nc = play_ply_eps_sched(c, rc, true, true);
+    if (na != nc || a.p1 != c.p1 || a.p2 != c.p2 || a.kings != c.kings || a.meta != c.meta || ra.k != rc.k) bad++;
+  }
+  return bad;
+}
+}

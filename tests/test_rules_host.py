@@ -94,3 +94,12 @@ def test_buffered_draw_schedule_replays_on_oracle(rh, policy):
         o = rh.rh_playout_ring(p.ctypes.data_as(u32p), 4242, i * 7, sparse_from, policy, pl.ctypes.data_as(u32p),
                                dr.ctypes.data_as(u32p))
         assert (o, int(pl[0]), int(dr[0])) == L.replay_one(p, 4242, i * 7, policy), (policy, i)
+
+
+def test_branch_free_eps_greedy_equals_enumeration(rh):
+    """The eps-greedy ply the kernels play without enumerating moves (best-move
+    masks, bit-sliced jump gains) picks the same move with the same draws as
+    the enumerating policy, on 300 K random boards with kings."""
+    rh.rh_eps_fast_matches_enum.restype = ctypes.c_long
+    rh.rh_eps_fast_matches_enum.argtypes = [ctypes.c_uint64, ctypes.c_uint64]
+    assert rh.rh_eps_fast_matches_enum(300_000, 17) == 0
