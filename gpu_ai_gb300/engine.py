@@ -71,8 +71,9 @@ def load_library(path: str = LIB_PATH):
     lib.gpuai_create.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)]
     lib.gpuai_destroy.argtypes = [ctypes.c_void_p]
     lib.gpuai_destroy.restype = None
-    lib.gpuai_playouts.argtypes = [ctypes.c_void_p, _u32p, _u32p, ctypes.c_uint32, ctypes.c_uint64,
-                                   ctypes.c_uint64, ctypes.c_int32, _i8p]
+    # raw addresses (ndarray.ctypes.data) for the array arguments: cheaper per call than data_as
+    lib.gpuai_playouts.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32,
+                                   ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int32, ctypes.c_void_p]
     lib.gpuai_playouts_device.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32,
                                           ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_uint64,
                                           ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p]
@@ -187,10 +188,9 @@ class Engine:
             if r.shape != (n,):
                 raise ValueError("reps must have one entry per board")
             total = int(r.sum(dtype=np.uint64))
-            rp = r.ctypes.data_as(_u32p)
+            rp = r.ctypes.data
         out = np.empty(total, dtype=np.int8)
-        _check(self.lib.gpuai_playouts(self.ctx, b.ctypes.data_as(_u32p), rp, n, seed, stream_base, policy,
-                                       out.ctypes.data_as(_i8p)))
+        _check(self.lib.gpuai_playouts(self.ctx, b.ctypes.data, rp, n, seed, stream_base, policy, out.ctypes.data))
         return out
 
     def playouts_device(self, d_pos: int, d_offsets: Optional[int], npos: int, uniform_reps: int, total: int,
