@@ -700,9 +700,8 @@ GA_HD int play_ply_men_multi(Board &b, const Side &s, const uint32_t J[4], Pick 
   return -1;  // unreachable: i < n
 }
 
-constexpr int kNeedSearch = -2;  // a men's multi-jump ply was deferred (kNeedMen)
-constexpr int kNeedMen = -2;
-constexpr int kNeedKing = -3;     // a ply where a king's capture can continue was deferred
+constexpr int kNeedMen = -2;   // a men's multi-jump ply was deferred
+constexpr int kNeedKing = -3;  // a ply where a king's capture can continue was deferred
 
 // Deferred-ply schedule of the uniform random playout kernel (iteration it of
 // its warp loop): Philox blocks are generated on it % 4 == 0, men's
@@ -762,11 +761,10 @@ GA_HD int play_ply_sched(Board &b, Pick &&pick, bool men_now, bool king_now) {
   return n;
 }
 
-// play_ply_sched with every rarer ply deferred (DEFER, returning kNeedMen or
-// kNeedKing) or played at once.
-template <bool DEFER = false, class Pick>
+// One uniformly random ply with every kind of ply played at once.
+template <class Pick>
 GA_HD int play_ply_fast(Board &b, Pick &&pick) {
-  return play_ply_sched(b, pick, !DEFER, !DEFER);
+  return play_ply_sched(b, pick, true, true);
 }
 
 // Random draws of one stream buffered eight at a time, so that a warp can
