@@ -149,6 +149,43 @@ def time_cpu_baseline(positions, min_seconds=10.0, max_seconds=30.0):
                       f"{el:.1f} s, HostPlayoutDriver (src/playout.cpp:17-32)"}
 
 
+def time_cpu_heuristic(positions, min_seconds=5.0):
+    """The reference's HostHeuristicPlayoutDriver (src/heuristicPlayout.cpp:12-48,
+    OpenMP over the states) on all of this machine's cores: built from the
+    reference's sources where they were present at build time, else the
+    oracle's restatement of it."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_lib as L
+    threads = os.cpu_count() or 1
+    run, kind = None, "port"
+    try:
+        if os.path.exists(L.REF_SO) and L.ref() is not None:
+            run, kind = L.host_heuristic_ref, "reference"
+    except OSError:
+        run = None
+    if run is None:
+        lib = L.oracle()
+        seed = [0]
+
+        def run(st):
+            st = np.ascontiguousarray(st, dtype=np.uint32)
+            out = np.zeros(st.shape[0], dtype=np.int8)
+            seed[0] += 1
+            lib.or_host_heuristic_playouts(L._ptr(st, L._u32p), st.shape[0], L._ptr(out, L._i8p), seed[0])
+            return out
+    chunk = np.repeat(positions, 16, axis=0)
+    done, t0 = 0, time.perf_counter()
+    while True:
+        run(chunk)
+        done += len(chunk)
+        el = time.perf_counter() - t0
+        if el >= min_seconds:
+            break
+    return {"value": done / el, "unit": UNIT, "cores": threads, "kind": kind,
+            "sample": f"{done} playouts of the same 64 positions, {el:.1f} s, HostHeuristicPlayoutDriver "
+                      "(src/heuristicPlayout.cpp:12-48)"}
+
+
 def dist_setup(n_gpus):
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -333,8 +370,29 @@ def run_ours(args):
         "clocks": clocks,
         "device": info,
     }
+    # the other playout policies on the same batch: device-resident, CUDA events
+    pols = {}
+    for pol, name in ((1, "ref_heuristic"), (2, "eps_greedy")):
+        ts, pl_sum = [], 0
+        for k in range(5):
+            flush.zero_()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            eng.playouts_device(d_pos.data_ptr(), None, N_POS, REPS, TOTAL, 0x5EED, base + (1000 + k) * TOTAL, pol,
+                                d_out.data_ptr(), sid)
+            b.record(stream)
+            st, pl = eng.status()
+            if st:
+                raise RuntimeError(f"kernel status {st}")
+            if k >= 2:
+                ts.append(a.elapsed_time(b) / 1e3)
+                pl_sum += pl
+        pols[name] = {"playouts_per_s": len(ts) * TOTAL / sum(ts), "ms_per_step": sum(ts) / len(ts) * 1e3,
+                      "plies_per_playout": pl_sum / (len(ts) * TOTAL)}
+    line["policies"] = pols
     if world == 1 and not args.no_cpu:
         line["cpu_baseline"] = time_cpu_baseline(positions)
+        pols["ref_heuristic"]["cpu_baseline"] = time_cpu_heuristic(positions)
     print(json.dumps(line), flush=True)
 
 

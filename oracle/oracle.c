@@ -10,6 +10,7 @@
 #include <stdlib.h>
 #include <string.h>
 #include <math.h>
+#include <stdatomic.h>
 #ifdef _OPENMP
 #include <omp.h>
 #endif
@@ -507,25 +508,53 @@ void or_host_playouts(const or_board16 *states, uint32_t n, int8_t *out, int nth
   (void)nthreads;
 }
 
-static inline uint64_t xs64(uint64_t *x) {
-  *x ^= *x << 13; *x ^= *x >> 7; *x ^= *x << 17; return *x;
+/* The noise source of HostHeuristicPlayoutDriver (heuristicPlayout.cpp:14-15):
+ * one std::default_random_engine (minstd_rand0: x = 16807 x mod 2^31 - 1) and
+ * one normal_distribution, shared by every OpenMP thread.  The reference
+ * shares them unsynchronised; here the shared words are read and written with
+ * relaxed atomic loads and stores, so the threads contend for the same cache
+ * lines without a data race (concurrent callers may repeat a draw, as they
+ * can in the reference).  N(0, sigma) by the polar method, the second deviate
+ * kept for the next call. */
+static _Atomic uint64_t g_engine = 1;
+static _Atomic int g_have_saved = 0;
+static _Atomic double g_saved = 0.0;
+
+static double engine_uniform(void) {
+  uint64_t x = atomic_load_explicit(&g_engine, memory_order_relaxed);
+  x = (x * 16807u) % 2147483647u;
+  atomic_store_explicit(&g_engine, x, memory_order_relaxed);
+  return (double)(x - 1) / 2147483646.0;
 }
-static float polar_normal(uint64_t *x, float sigma) {
+
+static float shared_normal(float sigma) {
+  if (atomic_load_explicit(&g_have_saved, memory_order_relaxed)) {
+    atomic_store_explicit(&g_have_saved, 0, memory_order_relaxed);
+    return (float)(atomic_load_explicit(&g_saved, memory_order_relaxed) * sigma);
+  }
   for (;;) {
-    double u = (double)(xs64(x) >> 11) * (1.0 / 9007199254740992.0) * 2.0 - 1.0;
-    double v = (double)(xs64(x) >> 11) * (1.0 / 9007199254740992.0) * 2.0 - 1.0;
-    double q = u * u + v * v;
-    if (q > 0.0 && q < 1.0) return (float)(u * sqrt(-2.0 * log(q) / q) * sigma);
+    const double u = 2.0 * engine_uniform() - 1.0, v = 2.0 * engine_uniform() - 1.0;
+    const double q = u * u + v * v;
+    if (q > 0.0 && q < 1.0) {
+      const double f = sqrt(-2.0 * log(q) / q);
+      atomic_store_explicit(&g_saved, u * f, memory_order_relaxed);
+      atomic_store_explicit(&g_have_saved, 1, memory_order_relaxed);
+      return (float)(v * f * sigma);
+    }
   }
 }
 
-/* HostHeuristicPlayoutDriver::runPlayouts (heuristicPlayout.cpp:12-48) */
+/* HostHeuristicPlayoutDriver::runPlayouts (heuristicPlayout.cpp:12-48):
+ * isGameOver() and getMoves() each generate the move list, every move is
+ * scored and weighted, and the noise comes from the shared engine above,
+ * restarted for each call (the reference constructs it per call). */
 void or_host_heuristic_playouts(const or_board16 *states, uint32_t n, int8_t *out, uint64_t seed) {
+  atomic_store(&g_engine, (uint64_t)(seed % 2147483646u) + 1u);
+  atomic_store(&g_have_saved, 0);
 #ifdef _OPENMP
 #pragma omp parallel for
 #endif
   for (int64_t i = 0; i < (int64_t)n; i++) {
-    uint64_t x = seed * 0x9E3779B97F4A7C15ull + (uint64_t)i * 0xD1B54A32D192ED03ull + 1;
     or_state s;
     or_from_board16(&states[i], &s);
     unsigned ss[2];
@@ -533,13 +562,15 @@ void or_host_heuristic_playouts(const or_board16 *states, uint32_t n, int8_t *ou
     for (;;) {
       int k;
       or_move *v = get_moves(&s, &k);
-      if (k == 0 || s.msc >= OR_DRAW_PLIES) { free(v); break; }
+      free(v);
+      if (k == 0 || s.msc >= OR_DRAW_PLIES) break;
+      v = get_moves(&s, &k);
       int best = -1, bms[2] = {0, 0};
       float bw = -INFINITY;
       for (int j = 0; j < k; j++) {
         int ms[2];
         or_score_move(&s, &v[j], ms);
-        float w = or_get_weight(&s, ss, ms) + polar_normal(&x, 0.11f);
+        float w = or_get_weight(&s, ss, ms) + shared_normal(0.11f);
         if (w > bw) { best = j; bw = w; bms[0] = ms[0]; bms[1] = ms[1]; }
       }
       or_apply(&s, &v[best]);

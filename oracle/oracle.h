@@ -111,9 +111,10 @@ void or_random_positions(uint64_t seed, uint32_t n, uint32_t min_plies, uint32_t
 void or_host_playouts(const or_board16 *states, uint32_t n, int8_t *out, int nthreads,
                       unsigned srand_seed);
 /* HostHeuristicPlayoutDriver::runPlayouts: argmax of heuristic weight plus
- * N(0, 0.11) noise.  The reference draws the noise from one engine shared by
- * all OpenMP threads; the restatement uses one xorshift stream per state and
- * the Marsaglia polar method, so it is a distributional restatement only. */
+ * N(0, 0.11) noise, the move list generated twice per ply, the noise drawn
+ * from one minstd engine shared by all OpenMP threads as in the reference.
+ * A restatement of the reference's cost structure; its outcomes agree with the
+ * reference's in distribution only. */
 void or_host_heuristic_playouts(const or_board16 *states, uint32_t n, int8_t *out,
                                 uint64_t seed);
 
