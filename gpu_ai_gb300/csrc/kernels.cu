@@ -93,12 +93,15 @@ __global__ void __launch_bounds__(BLOCK) playout_kernel(PlayoutArgs a) {
   uint32_t j = 0, plies_here = 0, game_plies = 0;
   bool have = false, exhausted = false;
 
-  if constexpr (POLICY == 0 || POLICY == 2) {
+  if constexpr (POLICY == 0 || POLICY == 1 || POLICY == 2) {
     // Uniform random policy: at most one draw per ply, so Philox blocks are
     // generated for the whole warp every fourth iteration (DrawRing keeps four
     // or more draws buffered) and new games start on those iterations too.
     // eps-greedy (policy 2, play_ply_eps_sched) takes at most two draws per
-    // ply and refills every second iteration.
+    // ply and refills every second iteration.  The reference heuristic
+    // (policy 1, play_ply_heur_sched) takes two draws per legal move: its ply
+    // loops over the moves for the warp's longest move list and refills the
+    // ring every second step, so Philox still runs for the whole warp at once.
     // Plies whose capture can be extended take longer code: men's multi-jumps
     // (about 2.6% of plies) are deferred to every kMenPeriod-th iteration and
     // plies where a king's capture can continue (about 0.7%, the costlier
@@ -149,8 +152,16 @@ __global__ void __launch_bounds__(BLOCK) playout_kernel(PlayoutArgs a) {
           break;
         }
         int n;
-        if constexpr (POLICY == 2) n = play_ply_eps_sched(b, rs, men_ok, king_ok);
-        else n = play_ply_sched(b, pick, men_ok, king_ok);
+        if constexpr (POLICY == 2) {
+          n = play_ply_eps_sched(b, rs, men_ok, king_ok);
+        } else if constexpr (POLICY == 1) {
+          RingOnDemand more{rs};
+          n = play_ply_heur_sched(
+              b, rs, more, men_ok, king_ok, [](uint32_t m) { return __reduce_max_sync(__activemask(), m); },
+              [&] { rs.refill(); });
+        } else {
+          n = play_ply_sched(b, pick, men_ok, king_ok);
+        }
         if (n == kNeedMen || n == kNeedKing) {
           pend = n == kNeedMen ? 1u : 2u;
           break;

@@ -812,6 +812,17 @@ struct DrawRing {
   }
 };
 
+// Draws from a DrawRing for code that may take any number of them: a block is
+// generated whenever fewer than four are buffered (for the rare plies that
+// enumerate their moves; the warp loop keeps Philox convergent otherwise).
+struct RingOnDemand {
+  DrawRing &r;
+  GA_HD uint32_t next() {
+    r.refill();
+    return r.next();
+  }
+};
+
 // ------------------------------------------------------------ per-ply policies
 // Each returns the number of legal moves (0: the side to move has lost), -1 on a limit.
 
@@ -1020,6 +1031,100 @@ GA_HD int play_ply_eps_sched(Board &b, Rng &rs, bool men_now, bool king_now) {
   uint32_t removed;
   nth_move(S0, S1, S2, S3, idx, capture, men, from, to, removed);
   apply_move(b, from, to, removed);
+  return n;
+}
+
+// ------------------------------------------------------------ reference heuristic, one step per move
+
+// The reference-heuristic ply (the move and the draws of ply_ref_heuristic)
+// for plies where no capture can continue: the ply's four material weights are
+// computed once (direct moves: with or without promotion; single jumps: a man
+// or a king captured, with or without promotion), then one loop step per move
+// in list order adds the move's noise (two draws) and keeps the first
+// maximum.  A cursor walks the source squares in order and each square's
+// directions in search order (men's captures dc = -1 first).  The loop runs
+// loop_n(n) >= n steps; steps past the ply's own moves do nothing, so the
+// lanes of a warp can run one common trip count, and refill() before every
+// even step keeps a ring of draws filled for the two draws per step.  Plies
+// where a capture can continue are deferred (kNeedMen / kNeedKing) or played
+// by ply_ref_heuristic with `more`, a source of draws that never runs dry.
+template <class Rng, class More, class LoopN, class Refill>
+GA_HD int play_ply_heur_sched(Board &b, Rng &rs, More &more, bool men_now, bool king_now, LoopN &&loop_n,
+                              Refill &&refill) {
+  Side s;
+  make_side(b, s);
+  const uint32_t men = s.own & ~s.ownK;
+  const uint32_t m01 = s.turn ? s.ownK : s.own;
+  const uint32_t m23 = s.turn ? s.own : s.ownK;
+  const uint32_t J0 = m01 & s.jd[0], J1 = m01 & s.jd[1], J2 = m23 & s.jd[2], J3 = m23 & s.jd[3];
+  const bool capture = (J0 | J1 | J2 | J3) != 0;
+  const uint32_t jall = s.jd[0] | s.jd[1] | s.jd[2] | s.jd[3];
+  const uint32_t jf = s.turn ? (s.jd[2] | s.jd[3]) : (s.jd[0] | s.jd[1]);
+  const uint32_t lm = jump2<0>(J0 & men) | jump2<1>(J1 & men) | jump2<2>(J2 & men) | jump2<3>(J3 & men);
+  const uint32_t lk = jump2<0>(J0 & s.ownK) | jump2<1>(J1 & s.ownK) | jump2<2>(J2 & s.ownK) |
+                      jump2<3>(J3 & s.ownK);
+  const uint32_t cont_k = lk & jall, cont_m = lm & jf;
+  if (cont_k | cont_m) {
+    if (cont_k && !king_now) return kNeedKing;
+    if (!cont_k && !men_now) return kNeedMen;
+    return ply_ref_heuristic(b, more);
+  }
+  const uint32_t M0 = capture ? J0 : (m01 & step<3>(s.empty)), M1 = capture ? J1 : (m01 & step<2>(s.empty));
+  const uint32_t M2 = capture ? J2 : (m23 & step<1>(s.empty)), M3 = capture ? J3 : (m23 & step<0>(s.empty));
+  const int n = popc(M0) + popc(M1) + popc(M2) + popc(M3);
+  if (n == 0) return 0;
+  const int ownScore = popc(s.own) + 3 * popc(s.ownK);
+  const int oppScore = popc(s.opp) + 3 * popc(s.opp & b.kings);
+  // weights: [promotes][captured piece is a king]; direct moves capture nothing
+  const int dm = capture ? 1 : 0, dk = capture ? 4 : 0;
+  const int32_t w00 = heur_weight_q16(ownScore, oppScore - dm), w01 = heur_weight_q16(ownScore, oppScore - dk);
+  const int32_t w10 = heur_weight_q16(ownScore + 3, oppScore - dm), w11 = heur_weight_q16(ownScore + 3, oppScore - dk);
+  // a man moving from these squares promotes (a step or a jump towards the far row)
+  const uint32_t promo = capture ? (s.turn ? 0x00000F00u : 0x00F00000u) : (s.turn ? 0x000000F0u : 0x0F000000u);
+  const uint32_t oppK = s.opp & b.kings;
+  int best_sq = -1, best_d = 0;
+  if (n == 1) {  // one move, no draws
+    best_sq = ctz(M0 | M1 | M2 | M3);
+    best_d = (int)ctz((((M0 >> best_sq) & 1u) | (((M1 >> best_sq) & 1u) << 1) | (((M2 >> best_sq) & 1u) << 2) |
+                       (((M3 >> best_sq) & 1u) << 3)));
+  } else {
+    uint32_t rest = M0 | M1 | M2 | M3;  // source squares still to visit
+    int sq = 0;
+    uint32_t dbits = 0;  // directions of sq still to visit, in search order
+    bool rev = false;    // dbits holds a man's captures: bit 0 is dc = -1
+    int32_t bw = 0;
+    const uint32_t steps = loop_n((uint32_t)n);
+    for (uint32_t k = 0; k < steps; k++) {
+      if ((k & 1u) == 0) refill();
+      if (k >= (uint32_t)n) continue;
+      if (dbits == 0) {
+        sq = ctz(rest);
+        rest &= rest - 1u;
+        const uint32_t x0 = (M0 >> sq) & 1u, x1 = (M1 >> sq) & 1u, x2 = (M2 >> sq) & 1u, x3 = (M3 >> sq) & 1u;
+        rev = capture && ((men >> sq) & 1u);
+        // a man's captures: P1 searches D1 then D0, P2 D3 then D2
+        dbits = rev ? (s.turn ? (x3 | (x2 << 1)) : (x1 | (x0 << 1))) : (x0 | (x1 << 1) | (x2 << 2) | (x3 << 3));
+      }
+      const uint32_t j = (0x12131210u >> (2u * dbits)) & 3u;  // lowest set bit of the 4-bit set
+      dbits &= dbits - 1u;
+      const int d = rev ? (s.turn ? 3 - (int)j : 1 - (int)j) : (int)j;
+      const uint32_t pr = ((promo & men) >> sq) & 1u;
+      const int mid = sq + step_off(sq, d);
+      const uint32_t ck = capture ? (oppK >> mid) & 1u : 0u;
+      int32_t w = pr ? (ck ? w11 : w10) : (ck ? w01 : w00);
+      const uint32_t x = rs.next();
+      const uint32_t y = rs.next();
+      w += heur_noise_q16(x, y);
+      if (best_sq < 0 || w > bw) {
+        best_sq = sq;
+        best_d = d;
+        bw = w;
+      }
+    }
+  }
+  const int mid = best_sq + step_off(best_sq, best_d);
+  const int to = capture ? best_sq + jump_off(best_d) : mid;
+  apply_move(b, best_sq, to, capture ? 1u << mid : 0u);
   return n;
 }
 

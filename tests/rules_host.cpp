@@ -64,9 +64,11 @@ int rh_playout(const uint32_t *pos, uint64_t seed, uint64_t id, int policy, uint
   return outcome;
 }
 
-// The same playout with the warp loop's schedule (uniform random policy 0 or
-// eps-greedy policy 2): Philox blocks generated every fourth (every second
-// for eps-greedy) iteration (DrawRing), men's multi-jumps and king
+// The same playout with the warp loop's schedule (uniform random policy 0,
+// reference heuristic 1, eps-greedy 2): Philox blocks generated every fourth
+// (every second for eps-greedy) iteration (DrawRing), the reference
+// heuristic's per-move loop run for more steps than the ply's moves (as for a
+// warp's longest move list) with its own refills, men's multi-jumps and king
 // capture searches deferred to their own iterations, as the warp loop does;
 // from iteration sparse_from on nothing is deferred (the kernel's schedule for
 // a warp left with few games).
@@ -86,7 +88,16 @@ int rh_playout_ring(const uint32_t *pos, uint64_t seed, uint64_t id, uint32_t sp
     const bool king_ok = sparse || (it & (kKingPeriod - 1u)) == kKingPhase;
     if ((pend == 1u && !men_ok) || (pend == 2u && !king_ok)) continue;
     if (((b.meta >> 8) & 0xffu) >= (uint32_t)kDrawPlies) { outcome = 0; break; }
-    const int n = policy == 2 ? play_ply_eps_sched(b, rs, men_ok, king_ok) : play_ply_sched(b, pick, men_ok, king_ok);
+    int n;
+    if (policy == 2) {
+      n = play_ply_eps_sched(b, rs, men_ok, king_ok);
+    } else if (policy == 1) {
+      RingOnDemand more{rs};
+      n = play_ply_heur_sched(b, rs, more, men_ok, king_ok, [&](uint32_t m) { return m + (uint32_t)(it % 3); },
+                              [&] { rs.refill(); });
+    } else {
+      n = play_ply_sched(b, pick, men_ok, king_ok);
+    }
     if (n == kNeedMen || n == kNeedKing) { pend = n == kNeedMen ? 1u : 2u; continue; }
     pend = 0;
     if (n == 0) { outcome = (b.meta & 1u) ? 1 : -1; break; }
@@ -141,6 +152,38 @@ long rh_eps_fast_matches_enum(uint64_t n, uint64_t seed) {
     rc.init(seed, t, 0);
     const int na = ply_eps_greedy(a, ra);
     const int nc = play_ply_eps_sched(c, rc, true, true);
+    if (na != nc || a.p1 != c.p1 || a.p2 != c.p2 || a.kings != c.kings || a.meta != c.meta || ra.k != rc.k) bad++;
+  }
+  return bad;
+}
+}
+
+extern "C" {
+// play_ply_heur_sched (loop run for n + t % 5 steps) against the enumerating
+// ply_ref_heuristic on n pseudo-random boards: same move count, board and
+// draws.  Returns the number of boards that differ.
+long rh_heur_fast_matches_enum(uint64_t n, uint64_t seed) {
+  uint64_t x = seed;
+  auto next = [&]() {
+    uint64_t z = (x += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+  };
+  long bad = 0;
+  for (uint64_t t = 0; t < n; t++) {
+    uint32_t occ = (uint32_t)next() & (uint32_t)next();
+    if (t & 1) occ |= (uint32_t)next() & (uint32_t)next();
+    const uint32_t side = (uint32_t)next();
+    const uint32_t kmask = t % 3 == 0 ? (uint32_t)next() : (t % 3 == 1 ? 0u : ~0u);
+    const Board b0 = {occ & side, occ & ~side, occ & kmask, (uint32_t)(next() & 1)};
+    Board a = b0, c = b0;
+    Stream ra, rc;
+    ra.init(seed, t, 0);
+    rc.init(seed, t, 0);
+    const int na = ply_ref_heuristic(a, ra);
+    const int nc = play_ply_heur_sched(c, rc, rc, true, true, [&](uint32_t m) { return m + (uint32_t)(t % 5); },
+                                       [] {});
     if (na != nc || a.p1 != c.p1 || a.p2 != c.p2 || a.kings != c.kings || a.meta != c.meta || ra.k != rc.k) bad++;
   }
   return bad;

@@ -80,11 +80,12 @@ def test_playouts_replay_on_oracle(rh, policy):
         assert (o, int(pl[0]), int(dr[0])) == L.replay_one(p, 77, 1000 + i, policy), (policy, i)
 
 
-@pytest.mark.parametrize("policy", [0, 2])
+@pytest.mark.parametrize("policy", [0, 1, 2])
 def test_buffered_draw_schedule_replays_on_oracle(rh, policy):
-    """The warp-synchronous Philox schedule of the random and eps-greedy
-    kernels (branch-free plies, deferred capture searches) consumes exactly the
-    stream the oracle replays."""
+    """The warp-synchronous Philox schedule of the playout kernel for every
+    policy (branch-free plies, the reference heuristic's per-move loop,
+    deferred capture searches) consumes exactly the stream the oracle
+    replays."""
     pos = np.concatenate([L.random_positions(12, 500, 0, 80), crafted_boards()])
     for i in range(3000):
         p = np.ascontiguousarray(pos[i % len(pos)])
@@ -103,3 +104,12 @@ def test_branch_free_eps_greedy_equals_enumeration(rh):
     rh.rh_eps_fast_matches_enum.restype = ctypes.c_long
     rh.rh_eps_fast_matches_enum.argtypes = [ctypes.c_uint64, ctypes.c_uint64]
     assert rh.rh_eps_fast_matches_enum(300_000, 17) == 0
+
+
+def test_one_step_per_move_reference_heuristic_equals_enumeration(rh):
+    """The reference-heuristic ply the kernels play with one loop step per move
+    picks the same move with the same draws as the enumerating policy, on
+    300 K random boards with kings."""
+    rh.rh_heur_fast_matches_enum.restype = ctypes.c_long
+    rh.rh_heur_fast_matches_enum.argtypes = [ctypes.c_uint64, ctypes.c_uint64]
+    assert rh.rh_heur_fast_matches_enum(300_000, 23) == 0
