@@ -2,11 +2,12 @@
 //
 // Thread-per-playout: each thread keeps its board as four 32-bit words in
 // registers and plays one ply per loop iteration.  The loop is warp-uniform:
-// a lane whose game ends writes its int8 outcome and, in the same iteration,
-// takes the next playout index from a warp-aggregated claim on a global work
-// counter, so the warp never waits for its longest game (the reference's
-// coarsePlayoutKernel work queue, src/coarsePlayout.cu:73-86, done with one
-// atomicAdd per warp claim instead of a per-thread atomicCAS spin).
+// a lane whose game ends writes its int8 outcome and, at the next refill
+// iteration (every fourth), takes the next playout index from a
+// warp-aggregated claim on a global work counter, so the warp never waits for
+// its longest game (the reference's coarsePlayoutKernel work queue,
+// src/coarsePlayout.cu:73-86, done with one atomicAdd per warp claim instead
+// of a per-thread atomicCAS spin).
 #include "launch.h"
 #include "rules.cuh"
 
@@ -58,30 +59,6 @@ __device__ __forceinline__ bool claim(const PlayoutArgs &a, bool have, uint32_t 
   return j < a.total;
 }
 
-// Play one ply of the lane's game; returns true when the game is over and
-// sets the outcome (+1 / -1 / 0).
-template <int POLICY, class Rng>
-__device__ __forceinline__ bool step_game(const PlayoutArgs &a, Board &b, Rng &rs, uint32_t &game_plies,
-                                          uint32_t &plies_here, int &outcome) {
-  outcome = 0;
-  if (((b.meta >> 8) & 0xffu) >= (uint32_t)kDrawPlies) return true;
-  const int n = ply<POLICY>(b, rs);
-  if (n == 0) {
-    outcome = (b.meta & 1u) ? 1 : -1;  // side to move cannot move and loses
-    return true;
-  }
-  if (n < 0) {
-    atomicOr(a.status, kStatusDepth);
-    return true;
-  }
-  if (++game_plies > kMaxPlies) {
-    atomicOr(a.status, kStatusPlyCap);
-    return true;
-  }
-  plies_here++;
-  return false;
-}
-
 template <int POLICY, int BLOCK>
 __global__ void __launch_bounds__(BLOCK) playout_kernel(PlayoutArgs a) {
   if (a.dev_sizes != nullptr) {
@@ -93,7 +70,8 @@ __global__ void __launch_bounds__(BLOCK) playout_kernel(PlayoutArgs a) {
   uint32_t j = 0, plies_here = 0, game_plies = 0;
   bool have = false, exhausted = false;
 
-  if constexpr (POLICY == 0 || POLICY == 1 || POLICY == 2) {
+  static_assert(POLICY >= 0 && POLICY <= 2, "policies: 0 random, 1 reference heuristic, 2 eps-greedy");
+  {
     // Uniform random policy: at most one draw per ply, so Philox blocks are
     // generated for the whole warp every fourth iteration (DrawRing keeps four
     // or more draws buffered) and new games start on those iterations too.
@@ -226,26 +204,6 @@ __global__ void __launch_bounds__(BLOCK) playout_kernel(PlayoutArgs a) {
         rs.b0 = s_slot[11][t]; rs.b1 = s_slot[12][t]; rs.b2 = s_slot[13][t]; rs.b3 = s_slot[14][t];
         rs.k = s_slot[15][t];
         rs.avail = s_slot[16][t];
-      }
-    }
-  } else {
-    Stream rs;
-    rs.init(0, 0, 0);
-    for (;;) {
-      if (claim(a, have, j, exhausted, lane)) {
-        have = true;
-        const uint32_t p = position_of(a, j);
-        b = load_board(a.pos + p);
-        rs.init(a.seed, stream_of(a, p, j), 0);
-        game_plies = 0;
-      }
-      if (!__any_sync(kFull, have)) break;
-      if (have) {
-        int outcome;
-        if (step_game<POLICY>(a, b, rs, game_plies, plies_here, outcome)) {
-          a.out[j] = (int8_t)outcome;
-          have = false;
-        }
       }
     }
   }
