@@ -907,7 +907,7 @@ GA_HD int ply_eps_greedy(Board &b, Rng &rs) {
 // ------------------------------------------------------------ eps-greedy without enumeration
 
 // Bit plane q of a per-square value c + sgn * row (4 squares per row).
-constexpr uint32_t row_value_plane(int q, int c, int sgn) {
+GA_HD constexpr uint32_t row_value_plane(int q, int c, int sgn) {
   uint32_t m = 0;
   for (int r = 0; r < 8; r++)
     if (((c + sgn * r) >> q) & 1) m |= 0xFu << (4 * r);
@@ -919,7 +919,7 @@ constexpr uint32_t row_value_plane(int q, int c, int sgn) {
 // advancement.  PLAYER_1 moving up (captured man one row above): 10 - row;
 // down: 12 - row; PLAYER_2 up: 5 + row; down: 3 + row.  Four bit planes each.
 struct RowValue { uint32_t q0, q1, q2, q3; };
-constexpr RowValue row_value(int c, int sgn) {
+GA_HD constexpr RowValue row_value(int c, int sgn) {
   return RowValue{row_value_plane(0, c, sgn), row_value_plane(1, c, sgn), row_value_plane(2, c, sgn),
                   row_value_plane(3, c, sgn)};
 }
