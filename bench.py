@@ -400,41 +400,53 @@ def run_searches(args):
     """Batched searches with device-resident trees: 2,048 games at U{0..60}
     random plies, playout budgets lognormal clipped to [1K, 256K], all advanced
     together; total playouts/s with graph-replayed steps and with eager
-    launches."""
+    launches.  Leaves per search start at --leaves and double (up to
+    --leaves-max) whenever the searches still running would put fewer
+    playouts into a step than the first step had: as the small budgets finish,
+    the large searches take more leaves per step instead of running
+    latency-bound steps of a few thousand playouts."""
     import torch
     from gpu_ai_gb300 import Engine, Searches
 
-    n_games, q, ppl = args.games, args.leaves, args.playouts_per_leaf
+    n_games, q, ppl, qmax = args.games, args.leaves, args.playouts_per_leaf, max(args.leaves, args.leaves_max)
     eng = Engine(0)
     roots = eng.random_positions(4242, n_games, 0, 60)
     rng = np.random.default_rng(4242)
     budgets = np.clip(np.exp(rng.normal(np.log(16384), 1.2, n_games)), 1024, 262144).astype(np.int64)
     budgets = (budgets + ppl - 1) // ppl * ppl
     caps = np.minimum(budgets, 131072).astype(np.int64) * 2
+    target = n_games * q * ppl  # playouts of the first step
     result = {}
     for mode in ("graph", "eager"):
-        s = Searches(n_games, int(caps.sum()) + 1024, q, playouts_per_leaf=ppl)
+        s = Searches(n_games, int(caps.sum()) + 1024, qmax, playouts_per_leaf=ppl)
         for i in range(n_games):
             s.add(roots[i], int(budgets[i]), int(caps[i]), i << 40)
         torch.cuda.synchronize()
-        steps = 0
+        steps, schedule = 0, {}
         t0 = time.perf_counter()
         while True:
             done, budget = s.poll()
-            if (done >= budget).all():
+            active = int((done < budget).sum())
+            if active == 0:
                 break
-            s.step(8, q, mode == "graph")
+            qq = q
+            while qq < qmax and active * qq * ppl < target:
+                qq *= 2
+            schedule[qq] = schedule.get(qq, 0) + 8
+            s.step(8, qq, mode == "graph")
             steps += 8
         el = time.perf_counter() - t0
         total = int(done.sum())
-        result[mode] = {"seconds": el, "steps": steps, "playouts": total, "playouts_per_s": total / el}
+        result[mode] = {"seconds": el, "steps": steps, "playouts": total, "playouts_per_s": total / el,
+                        "steps_by_leaves_per_search": {str(k): v for k, v in sorted(schedule.items())}}
         s.close()
     g, e = result["graph"], result["eager"]
     line = {
         "metric": "checkers playouts/sec, batched searches with device-resident trees", "value": g["playouts_per_s"],
         "unit": UNIT, "n_gpus": 1, "higher_is_better": True, "dtype": "u32", "data": "synthetic (seeded positions)",
         "config": {"workload": f"{n_games} games at 0-60 random plies, budgets lognormal in [1K, 256K]",
-                   "leaves_per_search_per_step": q, "playouts_per_leaf": ppl,
+                   "leaves_per_search_per_step": f"{q}, doubling up to {qmax} as searches finish",
+                   "playouts_per_leaf": ppl,
                    "total_budget": int(budgets.sum())},
         "graph": g, "eager": e,
         "launch_overhead_us_per_step": (e["seconds"] - g["seconds"]) / max(1, g["steps"]) * 1e6,
@@ -668,6 +680,8 @@ def main():
     ap.add_argument("--requests", type=int, default=2000, help="serve workload: number of requests")
     ap.add_argument("--games", type=int, default=2048, help="searches workload: number of games")
     ap.add_argument("--leaves", type=int, default=128, help="searches workload: leaves per search per step")
+    ap.add_argument("--leaves-max", type=int, default=512,
+                    help="searches workload: leaves per search per step once most searches have finished (<= 512)")
     ap.add_argument("--playouts-per-leaf", type=int, default=8, help="searches / mcts workloads: playouts per leaf")
     ap.add_argument("--ms-per-position", type=int, default=1000, help="mcts workload: search time per position")
     args = ap.parse_args()

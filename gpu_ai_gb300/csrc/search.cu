@@ -61,7 +61,7 @@ constexpr uint32_t kExpanded = 1u, kTerminal = 2u, kEvaluated = 4u;  // node sta
 constexpr int kMaxSelectDepth = 512;
 constexpr uint32_t kStatusSelectDepth = 8u;
 constexpr uint32_t kSelectWarps = 4;   // searches per select block
-constexpr uint32_t kMaxLeavesPerStep = 256;  // frontier capacity per search
+constexpr uint32_t kMaxLeavesPerStep = 512;  // frontier capacity per search (32 KB of static smem per select block)
 constexpr float kUcbC = 1.41421356f;
 constexpr int kMaxChildren = 64;  // moves per position handled by split_slots
 constexpr uint32_t kUnits = 64;   // learned searches: visit units per leaf slot (score2 = units * (1 + value))
@@ -649,7 +649,7 @@ int gpuai_searches_create(int device, uint32_t max_searches, uint32_t pool_nodes
     return err(GPUAI_ERR_INVALID, "gpuai_searches_create: zero size");
   if (policy < 0 || policy > 2) return err(GPUAI_ERR_INVALID, "gpuai_searches_create: unknown policy");
   if (max_leaves_per_step > kMaxLeavesPerStep)
-    return err(GPUAI_ERR_INVALID, "gpuai_searches_create: max_leaves_per_step above 256");
+    return err(GPUAI_ERR_INVALID, "gpuai_searches_create: max_leaves_per_step above 512");
   if ((uint64_t)max_searches * max_leaves_per_step * playouts_per_leaf > 0x7fffffffull || pool_nodes > 0x7fffffffu)
     return err(GPUAI_ERR_INVALID, "gpuai_searches_create: sizes exceed 2^31");
   int count = 0;

@@ -151,7 +151,7 @@ int gpuai_get_layout(gpuai_ctx *ctx, int32_t policy, int32_t *layout);
 typedef struct gpuai_searches gpuai_searches;
 
 /* pool_nodes: node capacity of the shared pool (52 bytes of device memory per
- * node); max_leaves_per_step bounds leaves_per_search. */
+ * node); max_leaves_per_step (at most 512) bounds leaves_per_search. */
 int gpuai_searches_create(int device, uint32_t max_searches, uint32_t pool_nodes, uint32_t max_leaves_per_step,
                           uint32_t playouts_per_leaf, int32_t policy, uint64_t seed, gpuai_searches **out);
 void gpuai_searches_destroy(gpuai_searches *s);

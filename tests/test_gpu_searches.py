@@ -96,3 +96,25 @@ def test_admission_by_free_node_range(lib_built):
     b = s.add(root, 100, 800, 2)
     run_to_end(s, q=8)
     assert s.children(b)["visits"].sum() == 100
+
+
+def test_wide_steps_of_512_leaves_per_search(lib_built):
+    """Steps of 512 leaf slots per search (the widest frontier the select step
+    holds): every playout is accounted for, the result is the same alone and
+    in a mix, and the tree keeps the root's legal moves."""
+    root = L.random_positions(12, 1, 20, 20)[0]
+    a = Searches(8, 600000, 512, playouts_per_leaf=2)
+    slot = a.add(root, 60000, 150000, 1 << 40)
+    done, budget = run_to_end(a, q=512)
+    assert done[slot] == budget[slot] == 60000
+    alone = stats(a, slot)
+    assert alone[0].sum() == 60000
+    legal, cnt = L.genmoves(root)
+    np.testing.assert_array_equal(alone[2], legal[0, :cnt[0]])
+    b = Searches(8, 600000, 512, playouts_per_leaf=2)
+    for i, r in enumerate(L.random_positions(13, 5, 0, 40)):
+        b.add(r, 9000 + 7000 * i, 40000, i << 32)
+    slot_b = b.add(root, 60000, 150000, 1 << 40)
+    run_to_end(b, q=512)
+    for x, y in zip(alone, stats(b, slot_b)):
+        np.testing.assert_array_equal(x, y)
