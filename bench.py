@@ -507,7 +507,7 @@ def run_serve(args):
     from gpu_ai_gb300.serve import simulate
     from gpu_ai_gb300 import POLICY_RANDOM, POLICY_REF_HEURISTIC
     res = {}
-    q = args.leaves if args.leaves <= 256 else 64
+    q = args.serve_leaves
     for name, pol in (("random", POLICY_RANDOM), ("ref_heuristic", POLICY_REF_HEURISTIC)):
         res[name] = simulate(rate=args.rate, n_requests=args.requests, n_games=10000, budget_ms=(10.0, 200.0),
                              policy=pol, leaves_per_search=q, playouts_per_leaf=args.playouts_per_leaf)
@@ -519,7 +519,7 @@ def run_serve(args):
             "value": res["random"]["latency_ms_p99"], "higher_is_better": False, "n_gpus": 1,
             "data": "synthetic (seeded games, Poisson arrivals)",
             "config": {"workload": f"{args.requests} requests at {args.rate} req/s, budgets U(10,200) ms",
-                       "leaves_per_search_per_step": args.leaves, "playouts_per_leaf": args.playouts_per_leaf},
+                       "leaves_per_search_per_step": q, "playouts_per_leaf": args.playouts_per_leaf},
             "random": res["random"], "ref_heuristic": res["ref_heuristic"], "learned": res["learned"]}
     print(json.dumps(line), flush=True)
 
@@ -677,6 +677,8 @@ def main():
     ap.add_argument("--match-games", type=int, default=400, help="learned workload: match games")
     ap.add_argument("--ms", type=float, default=100.0, help="learned workload: milliseconds per move")
     ap.add_argument("--rate", type=float, default=1000.0, help="serve workload: requests per second")
+    ap.add_argument("--serve-leaves", type=int, default=512,
+                    help="serve workload: leaves per search per step (1..512; every request gets the same)")
     ap.add_argument("--requests", type=int, default=2000, help="serve workload: number of requests")
     ap.add_argument("--games", type=int, default=2048, help="searches workload: number of games")
     ap.add_argument("--leaves", type=int, default=128, help="searches workload: leaves per search per step")
