@@ -176,8 +176,12 @@ class Engine:
             pass
 
     def playouts(self, pos, reps=None, seed: int = 0, stream_base: int = 0,
-                 policy: int = POLICY_RANDOM) -> np.ndarray:
-        """reps[p] playouts from pos[p] (one each if reps is None); int8 outcomes in order."""
+                 policy: int = POLICY_RANDOM, out: Optional[np.ndarray] = None) -> np.ndarray:
+        """reps[p] playouts from pos[p] (one each if reps is None); int8 outcomes in order.
+
+        `out`, if given, is a C-contiguous int8 array of exactly the number of
+        playouts that receives the outcomes (a caller running many batches can
+        reuse one buffer) and is returned."""
         b = _boards(pos)
         n = b.shape[0]
         if reps is None:
@@ -189,7 +193,10 @@ class Engine:
                 raise ValueError("reps must have one entry per board")
             total = int(r.sum(dtype=np.uint64))
             rp = r.ctypes.data
-        out = np.empty(total, dtype=np.int8)
+        if out is None:
+            out = np.empty(total, dtype=np.int8)
+        elif out.dtype != np.int8 or out.shape != (total,) or not out.flags.c_contiguous or not out.flags.writeable:
+            raise ValueError(f"out must be a writeable C-contiguous int8 array of {total} outcomes")
         _check(self.lib.gpuai_playouts(self.ctx, b.ctypes.data, rp, n, seed, stream_base, policy, out.ctypes.data))
         return out
 

@@ -42,6 +42,22 @@ def test_full_benchmark_batch_bit_exact(engine, golden_playout):
     assert plies == int(exp_plies.sum(dtype=np.uint64))
 
 
+
+def test_reused_out_buffer(engine):
+    """`out=` receives the same outcomes as a fresh array, is returned as is,
+    and a buffer of the wrong type, size or layout is refused before launch."""
+    pos = L.random_positions(9, 40, 0, 30)
+    reps = np.full(len(pos), 17, dtype=np.uint32)
+    exp = engine.playouts(pos, reps, seed=77, stream_base=5)
+    buf = np.full(exp.size, 99, dtype=np.int8)
+    got = engine.playouts(pos, reps, seed=77, stream_base=5, out=buf)
+    assert got is buf
+    np.testing.assert_array_equal(buf, exp)
+    for bad in (np.empty(exp.size, np.int16), np.empty(exp.size + 1, np.int8),
+                np.empty(2 * exp.size, np.int8)[::2]):
+        with pytest.raises(ValueError):
+            engine.playouts(pos, reps, seed=77, stream_base=5, out=bad)
+
 def test_outcome_frequencies_match_reference_host(engine, golden_playout):
     pos = golden_playout["positions"]
     reps = np.full(len(pos), int(golden_playout["reps"]), dtype=np.uint32)
