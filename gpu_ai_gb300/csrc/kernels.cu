@@ -59,8 +59,17 @@ __device__ __forceinline__ bool claim(const PlayoutArgs &a, bool have, uint32_t 
   return j < a.total;
 }
 
+// Resident blocks per SM that the register budget is sized for: 64 registers
+// a thread for blocks of 256 or more threads (80 for the reference heuristic
+// at 256: 3 blocks), 72 (96 for the reference heuristic) for smaller blocks.
 template <int POLICY, int BLOCK>
-__global__ void __launch_bounds__(BLOCK) playout_kernel(PlayoutArgs a) {
+constexpr int playout_min_blocks() {
+  constexpr int regs = BLOCK >= 256 ? (POLICY == 1 && BLOCK == 256 ? 80 : 64) : (POLICY == 1 ? 96 : 72);
+  return 65536 / (regs * BLOCK);
+}
+
+template <int POLICY, int BLOCK>
+__global__ void __launch_bounds__(BLOCK, (playout_min_blocks<POLICY, BLOCK>())) playout_kernel(PlayoutArgs a) {
   if (a.dev_sizes != nullptr) {
     a.npos = __ldg(&a.dev_sizes[0]);
     a.total = __ldg(&a.dev_sizes[1]);
@@ -96,12 +105,7 @@ __global__ void __launch_bounds__(BLOCK) playout_kernel(PlayoutArgs a) {
     constexpr int kWords = 17;
     __shared__ uint32_t s_slot[kWords][BLOCK];
     __shared__ uint32_t s_cnt[BLOCK / 32];
-    // exhaustion flag per parity of the compaction point, so that a warp
-    // setting it for the next point cannot race a slower warp's read
-    __shared__ uint32_t s_ex[2];
     const uint32_t warp = threadIdx.x >> 5;
-    if (threadIdx.x < 2) s_ex[threadIdx.x] = 0;
-    __syncthreads();
     DrawRing rs;
     rs.start(0, 0, 0);
     uint32_t pend = 0;    // deferred ply: 0 none, 1 men's multi-jump, 2 king capture search
@@ -164,10 +168,22 @@ __global__ void __launch_bounds__(BLOCK) playout_kernel(PlayoutArgs a) {
         }
         continue;
       }
-      const uint32_t parity = (it / kCompactPeriod) & 1u;
-      if (exhausted && lane == 0) s_ex[parity] = 1;
+      if (!exhausted) {
+        // A warp whose lanes are all busy makes no claims: it reads the work
+        // counter itself.  Counter values only grow, and a warp waits at the
+        // barrier below only after it saw the counter at or past the total, so
+        // every other warp of the block sees that too at its next compaction
+        // point and joins it: no barrier is needed while work remains.
+        uint32_t c = 0;
+        if (lane == 0) c = *reinterpret_cast<volatile const uint32_t *>(a.counter);
+        if (__shfl_sync(kFull, c, 0) < a.total) continue;  // warp-uniform
+        exhausted = true;
+      }
+      // Only warps that know the work is exhausted get here; they all pass the
+      // same sequence of compaction points (it % kCompactPeriod equal, absolute
+      // iteration counts may differ).  This barrier also keeps a fast warp from
+      // writing s_cnt for the next point while a slow one still reads it.
       __syncthreads();
-      if (!s_ex[parity]) continue;  // block-uniform: the work counter is not exhausted yet
       const uint32_t m = __ballot_sync(kFull, have);
       if (lane == 0) s_cnt[warp] = __popc(m);
       __syncthreads();
@@ -180,7 +196,6 @@ __global__ void __launch_bounds__(BLOCK) playout_kernel(PlayoutArgs a) {
         busy_warps += c ? 1u : 0u;
       }
       if (total == 0) break;
-      exhausted = true;
       sparse = __popc(m) <= kSparseLanes;
       if ((total + 31u) / 32u >= busy_warps) continue;  // packing would free no warp
       if (have) {
