@@ -53,7 +53,7 @@ WORKLOAD = {
 OPS_PER_PLY = 260.0
 # DRAM bytes per launch of the playout kernel from one ncu capture
 # (dram__bytes_read.sum + dram__bytes_write.sum).
-TRAFFIC_BYTES = 43776  # one ncu capture of the benchmark launch: 43.8 KB read, 0 B written
+TRAFFIC_BYTES = 44544  # one ncu capture of the benchmark launch: 44.0 KB read, 0.5 KB written
 
 
 def measured_peaks():
