@@ -12,6 +12,8 @@ streams (stream_base advances), so no step repeats work.
          host buffers: H2D of boards + offsets and D2H of outcomes every step
   roofline  integer-issue roofline of the playout kernel: plies/s x OPS_PER_PLY
          lane operations against SMs x 128 lanes x the maximum SM clock
+  clocks nvidia-smi samples (every 50 ms) that arrived during the timed
+         loop of `value`: median SM clock and active throttle reasons
   cpu_baseline  the reference's HostPlayoutDriver (built from its sources
          where present, else the oracle's restatement of it) on the host's
          cores, on a bounded sample of the same positions
@@ -65,7 +67,9 @@ def measured_peaks():
 
 
 class ClockSampler:
-    """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
+    """nvidia-smi clocks / throttle reasons sampled every 50 ms; stop(t0, t1)
+    keeps the samples that arrived inside the timed window [t0, t1]
+    (perf_counter seconds)."""
 
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -75,7 +79,7 @@ class ClockSampler:
     def __init__(self, bus_id=None):
         self.rows = []
         self.proc = None
-        cmd = ["nvidia-smi", "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits", "-lms", "200"]
+        cmd = ["nvidia-smi", "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits", "-lms", "50"]
         if bus_id:
             cmd += ["-i", bus_id]
         try:
@@ -89,26 +93,32 @@ class ClockSampler:
         for line in self.proc.stdout:
             parts = [p.strip() for p in line.split(",")]
             if len(parts) >= 9:
-                self.rows.append(parts)
+                self.rows.append((time.perf_counter(), parts))
 
-    def stop(self):
+    def wait_first(self, timeout=5.0):
+        """Block until nvidia-smi has printed its first sample (or timeout)."""
+        end = time.perf_counter() + timeout
+        while self.proc and not self.rows and time.perf_counter() < end:
+            time.sleep(0.01)
+
+    def stop(self, t0=None, t1=None):
         if not self.proc:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
-        time.sleep(0.3)
         self.proc.terminate()
         try:
             self.proc.wait(timeout=5)
         except subprocess.TimeoutExpired:
             self.proc.kill()
-        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
-        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        rows = [r for t, r in self.rows if t0 is None or t0 <= t <= t1]
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
         reasons = set()
-        for r in self.rows:
+        for r in rows:
             for name, v in zip(self.NAMES, r[5:9]):
                 if v.lower() == "active":
                     reasons.add(name)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": sorted(reasons), "samples": len(self.rows)}
+                "reasons": sorted(reasons), "samples": len(rows), "window_s": (t1 - t0) if t0 is not None else None}
 
 
 def cpu_reference_runner():
@@ -304,6 +314,7 @@ def run_ours(args):
     barrier(world)
     torch.cuda.synchronize()
     sampler = ClockSampler(bus)
+    sampler.wait_first()
     wall0 = time.perf_counter()
     for k in range(args.steps):
         flush.zero_()
@@ -315,9 +326,10 @@ def run_ours(args):
             raise RuntimeError(f"kernel status {st}")
         plies += pl
     torch.cuda.synchronize()
-    wall = time.perf_counter() - wall0
+    wall1 = time.perf_counter()
+    wall = wall1 - wall0
     barrier(world)
-    clocks = sampler.stop()
+    clocks = sampler.stop(wall0, wall1)
     kern_s = sum(a.elapsed_time(b) for a, b in ev) / 1e3
     kern_s_max = max_over_ranks(kern_s, world)
     value = world * args.steps * TOTAL / kern_s_max
@@ -660,7 +672,9 @@ def run_learned(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=None,
+                    help="timed steps (default: 2000 for the playouts workload, so that the timed region spans "
+                         "about a second of clock samples; 20 for the reference arm and the other workloads)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
@@ -688,6 +702,10 @@ def main():
     ap.add_argument("--playouts-per-leaf", type=int, default=8, help="searches / mcts workloads: playouts per leaf")
     ap.add_argument("--ms-per-position", type=int, default=1000, help="mcts workload: search time per position")
     args = ap.parse_args()
+    if args.steps is None:
+        args.steps = 2000 if args.impl == "ours" and args.workload == "playouts" else 20
+    if args.steps < 1:
+        ap.error("--steps must be >= 1")
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
     if args.impl == "reference":

@@ -46,7 +46,7 @@ def test_two_gloo_ranks_barrier_and_max():
     assert [r for r, *_ in res] == [0, 1]
     assert all(w == 2 and m == 2.5 for _, w, m, _ in res)
     bases = [b for *_, b in res]
-    steps_playouts = 1000 * 64 * 4096  # far more than any bench run
+    steps_playouts = 100_000 * 64 * 4096  # far more than any bench run (2,003 steps by default)
     assert bases[1] - bases[0] > steps_playouts
 
 
