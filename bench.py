@@ -109,16 +109,22 @@ class ClockSampler:
             self.proc.wait(timeout=5)
         except subprocess.TimeoutExpired:
             self.proc.kill()
-        rows = [r for t, r in self.rows if t0 is None or t0 <= t <= t1]
-        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
-        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
-        reasons = set()
-        for r in rows:
-            for name, v in zip(self.NAMES, r[5:9]):
-                if v.lower() == "active":
-                    reasons.add(name)
-        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": sorted(reasons), "samples": len(rows), "window_s": (t1 - t0) if t0 is not None else None}
+        return summarize_clocks(self.rows, t0, t1)
+
+
+def summarize_clocks(rows, t0=None, t1=None):
+    """(arrival time, nvidia-smi fields) rows -> the `clocks` object: median SM
+    clock, maximum SM clock and throttle reasons of the rows inside [t0, t1]."""
+    rows = [r for t, r in rows if t0 is None or t0 <= t <= t1]
+    sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+    mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+    reasons = set()
+    for r in rows:
+        for name, v in zip(ClockSampler.NAMES, r[5:9]):
+            if v.lower() == "active":
+                reasons.add(name)
+    return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+            "reasons": sorted(reasons), "samples": len(rows), "window_s": (t1 - t0) if t0 is not None else None}
 
 
 def cpu_reference_runner():
