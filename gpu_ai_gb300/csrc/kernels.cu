@@ -110,6 +110,7 @@ __global__ void __launch_bounds__(BLOCK, (playout_min_blocks<POLICY, BLOCK>())) 
     rs.start(0, 0, 0);
     uint32_t pend = 0;    // deferred ply: 0 none, 1 men's multi-jump, 2 king capture search
     bool sparse = false;  // warp-uniform: the work ran out and the warp holds kSparseLanes games or fewer
+    auto pick = [&](uint32_t n) { return rs.pick(n); };
     constexpr uint32_t kRefillMask = POLICY == 2 ? 1u : 3u;
     for (uint32_t it = 0;; ++it) {
       if ((it & kRefillMask) == 0) {
@@ -141,7 +142,7 @@ __global__ void __launch_bounds__(BLOCK, (playout_min_blocks<POLICY, BLOCK>())) 
               b, rs, more, men_ok, king_ok, [](uint32_t m) { return __reduce_max_sync(__activemask(), m); },
               [&] { rs.refill(); });
         } else {
-          n = play_ply_sched_ring(b, rs, men_ok, king_ok);
+          n = play_ply_sched(b, pick, men_ok, king_ok);
         }
         if (n == kNeedMen || n == kNeedKing) {
           pend = n == kNeedMen ? 1u : 2u;

@@ -25,13 +25,9 @@
 
 #if defined(__CUDACC__)
 #define GA_HD __host__ __device__ __forceinline__
-// kept out of line: rare code whose registers should not count against the
-// loop that calls it (internal linkage, one copy per translation unit)
-#define GA_COLD static __host__ __device__ __noinline__
 #define GA_UNROLL _Pragma("unroll")
 #else
 #define GA_HD inline
-#define GA_COLD static inline
 #define GA_UNROLL
 #endif
 
@@ -717,65 +713,16 @@ constexpr uint32_t kMenPeriod = 4, kMenPhase = 2;
 constexpr uint32_t kKingPeriod = 16, kKingPhase = 6;
 constexpr uint32_t kSparseLanes = 4;
 
-// A uniformly random ply where some capture can continue: the bit-sliced
-// men's tree (play_ply_men_multi) when only men continue, else the
-// depth-first search with the cycle check (play_ply).  Returns the move count.
-template <class Pick>
-GA_HD int play_ply_cont(Board &b, bool king, Pick &&pick) {
-  if (king) return play_ply(b, pick);
-  Side s;
-  make_side(b, s);
-  const uint32_t m01 = s.turn ? s.ownK : s.own;
-  const uint32_t m23 = s.turn ? s.own : s.ownK;
-  const uint32_t J[4] = {m01 & s.jd[0], m01 & s.jd[1], m23 & s.jd[2], m23 & s.jd[3]};
-  return s.turn ? play_ply_men_multi<3, 2>(b, s, J, pick) : play_ply_men_multi<1, 0>(b, s, J, pick);
-}
-
-struct ContOut {
-  uint32_t p1, p2, kings, meta;
-  int n;
-};
-
-// play_ply_cont out of line, on the board words by value, with r the draw
-// the ply uses when it has two or more moves.  The rare plies then keep their
-// registers to themselves: the playout loop that calls this is register-bound.
-GA_COLD ContOut play_ply_cont_cold(uint32_t p1, uint32_t p2, uint32_t kings, uint32_t meta, uint32_t r, bool king) {
-  Board b;
-  b.p1 = p1; b.p2 = p2; b.kings = kings; b.meta = meta;
-  const int n = play_ply_cont(b, king, [r](uint32_t m) { return m >= 2 ? mulhi_index(r, m) : 0u; });
-  return ContOut{b.p1, b.p2, b.kings, b.meta, n};
-}
-
-// Draw sources of play_ply_sched_with: `pick(n)` gives the index of the move
-// played among n, `cont(b, king)` plays a ply where a capture can continue.
-template <class Pick>
-struct InlineDraws {
-  Pick &pick_;
-  GA_HD uint32_t pick(uint32_t n) { return pick_(n); }
-  GA_HD int cont(Board &b, bool king) { return play_ply_cont(b, king, pick_); }
-};
-
-template <class Ring>
-struct RingDraws {
-  Ring &ring;
-  GA_HD uint32_t pick(uint32_t n) { return ring.pick(n); }
-  GA_HD int cont(Board &b, bool king) {
-    const ContOut o = play_ply_cont_cold(b.p1, b.p2, b.kings, b.meta, ring.peek(), king);
-    b.p1 = o.p1; b.p2 = o.p2; b.kings = o.kings; b.meta = o.meta;
-    ring.consume(o.n >= 2);  // a draw is used only with two or more moves, as in pick
-    return o.n;
-  }
-};
-
 // One uniformly random ply, branch-free for direct moves and for captures
 // that cannot be extended (the common cases).  Positions where some capture
-// can continue go to draws.cont (play_ply_cont).  A caller that batches these
-// rarer plies passes men_now / king_now = false: the ply then returns
-// kNeedMen / kNeedKing without touching the board or the stream, and is
-// played by a later call that allows it.  Same move list order, same
-// index -> move map as play_ply.
-template <class Draws>
-GA_HD int play_ply_sched_with(Board &b, Draws &&draws, bool men_now, bool king_now) {
+// can continue take the bit-sliced men's tree (play_ply_men_multi) when only
+// men continue, or the depth-first search with the cycle check (play_ply)
+// when a king does.  A caller that batches these rarer plies passes
+// men_now / king_now = false: the ply then returns kNeedMen / kNeedKing
+// without touching the board or the stream, and is played by a later call
+// that allows it.  Same move list order, same index -> move map as play_ply.
+template <class Pick>
+GA_HD int play_ply_sched(Board &b, Pick &&pick, bool men_now, bool king_now) {
   Side s;
   make_side(b, s);
   const uint32_t men = s.own & ~s.ownK;
@@ -791,8 +738,14 @@ GA_HD int play_ply_sched_with(Board &b, Draws &&draws, bool men_now, bool king_n
                       jump2<3>(J3 & s.ownK);
   const uint32_t cont_k = lk & jall, cont_m = lm & jf;
   if (cont_k | cont_m) {
-    if (cont_k ? !king_now : !men_now) return cont_k ? kNeedKing : kNeedMen;
-    return draws.cont(b, cont_k != 0);
+    if (cont_k) {
+      if (!king_now) return kNeedKing;
+      return play_ply(b, pick);  // a king can continue: depth-first search with the cycle check
+    }
+    if (!men_now) return kNeedMen;
+    // only men continue: counted on the bit-sliced continuation tree
+    const uint32_t J[4] = {J0, J1, J2, J3};
+    return s.turn ? play_ply_men_multi<3, 2>(b, s, J, pick) : play_ply_men_multi<1, 0>(b, s, J, pick);
   }
   const uint32_t M0 = capture ? J0 : (m01 & step<3>(s.empty));
   const uint32_t M1 = capture ? J1 : (m01 & step<2>(s.empty));
@@ -800,26 +753,12 @@ GA_HD int play_ply_sched_with(Board &b, Draws &&draws, bool men_now, bool king_n
   const uint32_t M3 = capture ? J3 : (m23 & step<0>(s.empty));
   const int n = popc(M0) + popc(M1) + popc(M2) + popc(M3);
   if (n == 0) return 0;
-  const uint32_t i = draws.pick((uint32_t)n);
+  const uint32_t i = pick((uint32_t)n);
   int from, to;
   uint32_t removed;
   nth_move(M0, M1, M2, M3, i, capture, men, from, to, removed);
   apply_move(b, from, to, removed);
   return n;
-}
-
-// play_ply_sched_with on a move-index function pick(n), every ply inline.
-template <class Pick>
-GA_HD int play_ply_sched(Board &b, Pick &&pick, bool men_now, bool king_now) {
-  return play_ply_sched_with(b, InlineDraws<Pick>{pick}, men_now, king_now);
-}
-
-// play_ply_sched_with on a DrawRing (the playout kernel's stream), the plies
-// where a capture can continue out of line.  Same moves and draws as
-// play_ply_sched with pick = ring.pick.
-template <class Ring>
-GA_HD int play_ply_sched_ring(Board &b, Ring &ring, bool men_now, bool king_now) {
-  return play_ply_sched_with(b, RingDraws<Ring>{ring}, men_now, king_now);
 }
 
 // One uniformly random ply with every kind of ply played at once.
@@ -861,17 +800,6 @@ struct DrawRing {
     k += use;
     avail -= use;
     return use ? mulhi_index(r, n) : 0u;
-  }
-  // The draw pick() would use next, without consuming it.
-  GA_HD uint32_t peek() const {
-    const bool hi = (k & 4u) != 0;
-    const uint32_t w = k & 3u;
-    const uint32_t x0 = hi ? b0 : a0, x1 = hi ? b1 : a1, x2 = hi ? b2 : a2, x3 = hi ? b3 : a3;
-    return w == 0 ? x0 : (w == 1 ? x1 : (w == 2 ? x2 : x3));
-  }
-  GA_HD void consume(bool use) {
-    k += use ? 1u : 0u;
-    avail -= use ? 1u : 0u;
   }
   GA_HD uint32_t next() {
     const bool hi = (k & 4u) != 0;

@@ -77,6 +77,7 @@ int rh_playout_ring(const uint32_t *pos, uint64_t seed, uint64_t id, uint32_t sp
   Board b = load(pos);
   DrawRing rs;
   rs.start(seed, id, 0);
+  auto pick = [&](uint32_t n) { return rs.pick(n); };
   uint32_t p = 0;
   int outcome = 0;
   uint32_t pend = 0;
@@ -95,7 +96,7 @@ int rh_playout_ring(const uint32_t *pos, uint64_t seed, uint64_t id, uint32_t sp
       n = play_ply_heur_sched(b, rs, more, men_ok, king_ok, [&](uint32_t m) { return m + (uint32_t)(it % 3); },
                               [&] { rs.refill(); });
     } else {
-      n = play_ply_sched_ring(b, rs, men_ok, king_ok);
+      n = play_ply_sched(b, pick, men_ok, king_ok);
     }
     if (n == kNeedMen || n == kNeedKing) { pend = n == kNeedMen ? 1u : 2u; continue; }
     pend = 0;
@@ -106,52 +107,6 @@ int rh_playout_ring(const uint32_t *pos, uint64_t seed, uint64_t id, uint32_t sp
   if (plies) *plies = p;
   if (draws) *draws = rs.k;
   return outcome;
-}
-
-// play_ply_sched_ring (the kernel's form: plies where a capture can continue
-// out of line, on the ring's next draw) against play_ply_sched with
-// pick = ring.pick, ply by ply over `games` random games from the start under
-// the kernel's deferral schedule: same move count, board and draws.  Returns
-// the number of mismatching plies; *plies / *deferred count what was compared.
-uint32_t rh_ring_matches_inline(uint64_t seed, uint32_t games, uint64_t *plies, uint64_t *deferred) {
-  uint32_t bad = 0;
-  uint64_t np = 0, nd = 0;
-  for (uint32_t g = 0; g < games; g++) {
-    Board a = {0x00000FFFu, 0xFFF00000u, 0u, 0u}, b = a;
-    DrawRing ra, rb;
-    ra.start(seed, g, 0);
-    rb.start(seed, g, 0);
-    auto pick = [&](uint32_t n) { return ra.pick(n); };
-    uint32_t pend = 0;
-    for (uint32_t it = 0; it < 16384u; ++it) {  // games end by the 50-ply rule long before
-      if ((it & 3u) == 0) {
-        ra.refill();
-        rb.refill();
-      }
-      const bool men_ok = g % 5 == 0 || (it & (kMenPeriod - 1u)) == kMenPhase;
-      const bool king_ok = g % 7 == 0 || (it & (kKingPeriod - 1u)) == kKingPhase;
-      if ((pend == 1u && !men_ok) || (pend == 2u && !king_ok)) continue;
-      if (((a.meta >> 8) & 0xffu) >= (uint32_t)kDrawPlies) break;
-      const int na = play_ply_sched(a, pick, men_ok, king_ok);
-      const int nb = play_ply_sched_ring(b, rb, men_ok, king_ok);
-      if (na != nb || a.p1 != b.p1 || a.p2 != b.p2 || a.kings != b.kings || a.meta != b.meta || ra.k != rb.k ||
-          ra.avail != rb.avail) {
-        bad++;
-        break;
-      }
-      if (na == kNeedMen || na == kNeedKing) {
-        pend = na == kNeedMen ? 1u : 2u;
-        nd++;
-        continue;
-      }
-      pend = 0;
-      if (na <= 0) break;
-      np++;
-    }
-  }
-  if (plies) *plies = np;
-  if (deferred) *deferred = nd;
-  return bad;
 }
 
 void rh_random_positions(uint64_t seed, uint32_t n, uint32_t min_plies, uint32_t max_plies,

@@ -97,19 +97,6 @@ def test_buffered_draw_schedule_replays_on_oracle(rh, policy):
         assert (o, int(pl[0]), int(dr[0])) == L.replay_one(p, 4242, i * 7, policy), (policy, i)
 
 
-def test_out_of_line_continuing_captures_equal_inline(rh):
-    """The playout kernel plays plies where a capture can continue out of line,
-    on the ring's next draw (play_ply_sched_ring); ply by ply over 200 K random
-    games under the deferral schedule, it plays the same moves with the same
-    draws as the inline form (play_ply_sched on ring.pick)."""
-    rh.rh_ring_matches_inline.restype = ctypes.c_uint32
-    rh.rh_ring_matches_inline.argtypes = [ctypes.c_uint64, ctypes.c_uint32, ctypes.POINTER(ctypes.c_uint64),
-                                          ctypes.POINTER(ctypes.c_uint64)]
-    plies, deferred = ctypes.c_uint64(), ctypes.c_uint64()
-    assert rh.rh_ring_matches_inline(0xC01D, 200_000, ctypes.byref(plies), ctypes.byref(deferred)) == 0
-    assert plies.value > 10_000_000 and deferred.value > 100_000
-
-
 def test_branch_free_eps_greedy_equals_enumeration(rh):
     """The eps-greedy ply the kernels play without enumerating moves (best-move
     masks, bit-sliced jump gains) picks the same move with the same draws as
