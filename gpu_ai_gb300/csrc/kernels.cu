@@ -92,7 +92,7 @@ __global__ void __launch_bounds__(BLOCK, (playout_min_blocks<POLICY, BLOCK>())) 
     // Plies whose capture can be extended take longer code: men's multi-jumps
     // (about 2.6% of plies) are deferred to every kMenPeriod-th iteration and
     // plies where a king's capture can continue (about 0.7%, the costlier
-    // depth-first search) to every kKingPeriod-th, so that the lanes needing
+    // depth-first search) to every king_period(POLICY)-th, so that the lanes needing
     // that code run it together and the other iterations stay branch-free.
     // Once the work counter is exhausted, a warp with kSparseLanes or fewer
     // games defers nothing: its few games are latency-bound.
@@ -124,7 +124,7 @@ __global__ void __launch_bounds__(BLOCK, (playout_min_blocks<POLICY, BLOCK>())) 
         if (have) rs.refill();
       }
       const bool men_ok = sparse || (it & (kMenPeriod - 1u)) == kMenPhase;
-      const bool king_ok = sparse || (it & (kKingPeriod - 1u)) == kKingPhase;
+      const bool king_ok = sparse || (it & (king_period(POLICY) - 1u)) == kKingPhase;
       do {
         if (!have) break;
         if ((pend == 1u && !men_ok) || (pend == 2u && !king_ok)) break;  // still deferred

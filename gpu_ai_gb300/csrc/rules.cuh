@@ -703,14 +703,17 @@ GA_HD int play_ply_men_multi(Board &b, const Side &s, const uint32_t J[4], Pick 
 constexpr int kNeedMen = -2;   // a men's multi-jump ply was deferred
 constexpr int kNeedKing = -3;  // a ply where a king's capture can continue was deferred
 
-// Deferred-ply schedule of the uniform random playout kernel (iteration it of
-// its warp loop): Philox blocks are generated on it % 4 == 0, men's
-// multi-jumps are played on it % kMenPeriod == kMenPhase, king capture
-// searches on it % kKingPeriod == kKingPhase (powers of 2, phases away from
-// the refill and the compaction iterations); once the work runs out, a warp
-// with at most kSparseLanes games defers nothing.
+// Deferred-ply schedule of the playout kernel (iteration it of its warp
+// loop): Philox blocks are generated on it % 4 == 0 (it % 2 == 0 for
+// eps-greedy), men's multi-jumps are played on it % kMenPeriod == kMenPhase,
+// king capture searches on it % king_period(policy) == kKingPhase (powers of
+// 2, phases away from the refill and the compaction iterations); once the
+// work runs out, a warp with at most kSparseLanes games defers nothing.  The
+// uniform random policy waits longer for king searches (16 iterations) than
+// the other two (8), whose plies cost more and leave fewer lanes waiting.
 constexpr uint32_t kMenPeriod = 4, kMenPhase = 2;
 constexpr uint32_t kKingPeriod = 16, kKingPhase = 6;
+GA_HD constexpr uint32_t king_period(int policy) { return policy == 0 ? kKingPeriod : kKingPeriod / 2; }
 constexpr uint32_t kSparseLanes = 4;
 
 // One uniformly random ply, branch-free for direct moves and for captures

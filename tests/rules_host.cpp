@@ -85,7 +85,7 @@ int rh_playout_ring(const uint32_t *pos, uint64_t seed, uint64_t id, uint32_t sp
     if ((it & (policy == 2 ? 1u : 3u)) == 0) rs.refill();  // eps-greedy takes up to two draws per ply
     const bool sparse = it >= sparse_from;
     const bool men_ok = sparse || (it & (kMenPeriod - 1u)) == kMenPhase;
-    const bool king_ok = sparse || (it & (kKingPeriod - 1u)) == kKingPhase;
+    const bool king_ok = sparse || (it & (king_period(policy) - 1u)) == kKingPhase;
     if ((pend == 1u && !men_ok) || (pend == 2u && !king_ok)) continue;
     if (((b.meta >> 8) & 0xffu) >= (uint32_t)kDrawPlies) { outcome = 0; break; }
     int n;
