@@ -61,15 +61,21 @@ class SearchServer:
     def __init__(self, max_searches: int = 4096, pool_nodes: Optional[int] = None, pool_fraction: float = 0.25,
                  leaves_per_search: int = 64, playouts_per_leaf: int = 8, policy: int = POLICY_RANDOM,
                  seed: int = 0, use_graph: bool = True, steps_per_poll: int = 2, net=None,
-                 value_weight: float = 0.5, c_puct: float = 1.5):
+                 value_weight: float = 0.5, c_puct: float = 1.5, searches=None):
+        """`searches`: an already created search pool with the `Searches`
+        interface (try_add / step / poll / best / remove / close) to serve
+        from instead of creating one; pool_nodes must then be given."""
         node_bytes = NODE_BYTES + (LEARNED_NODE_BYTES if net is not None else 0)
         if pool_nodes is None:  # admission by free device memory
+            if searches is not None:
+                raise ValueError("pool_nodes is required with an existing search pool")
             import torch
             free, _ = torch.cuda.mem_get_info()
             pool_nodes = int(free * pool_fraction) // node_bytes
         self.pool_nodes = pool_nodes
         self.node_bytes = node_bytes
-        self.s = Searches(max_searches, pool_nodes, leaves_per_search, playouts_per_leaf, policy, seed)
+        self.s = searches if searches is not None else Searches(max_searches, pool_nodes, leaves_per_search,
+                                                                playouts_per_leaf, policy, seed)
         if net is not None:  # learned searches: network leaf values and move priors
             self.s.set_net(net, value_weight, c_puct)
         self.q = leaves_per_search
