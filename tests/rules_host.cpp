@@ -131,6 +131,55 @@ extern "C" {
 // ply_eps_greedy on n pseudo-random boards (any occupancy, kings included,
 // seeded splitmix64): same move count, same board after the ply, same draws.
 // Returns the number of boards that differ.
+// play_ply_sched (every ply allowed) against the depth-first play_ply on n
+// pseudo-random boards: same move count, board and draws.  *forced counts the
+// boards whose ply was a men's multi-jump with one legal move, which
+// play_forced_men_multi plays without the men's tree.  Returns the number of
+// boards that differ.
+long rh_random_fast_matches_dfs(uint64_t n, uint64_t seed, uint64_t *forced) {
+  uint64_t x = seed;
+  auto next = [&]() {
+    uint64_t z = (x += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+  };
+  long bad = 0;
+  uint64_t nf = 0;
+  for (uint64_t t = 0; t < n; t++) {
+    uint32_t occ = (uint32_t)next() & (uint32_t)next();
+    if (t & 1) occ |= (uint32_t)next() & (uint32_t)next();
+    const uint32_t side = (uint32_t)next();
+    const uint32_t kmask = t % 3 == 0 ? (uint32_t)next() : (t % 3 == 1 ? 0u : (uint32_t)next() & (uint32_t)next());
+    const Board b0 = {occ & side, occ & ~side, occ & kmask, (uint32_t)(next() & 1)};
+    Board a = b0, c = b0, f = b0;
+    DrawRing ra, rc;
+    ra.start(seed, t, 0);
+    rc.start(seed, t, 0);
+    ra.refill();
+    rc.refill();
+    const int na = play_ply_sched(a, [&](uint32_t m) { return ra.pick(m); }, true, true);
+    const int nc = play_ply(c, [&](uint32_t m) { return rc.pick(m); });
+    if (na != nc || a.p1 != c.p1 || a.p2 != c.p2 || a.kings != c.kings || a.meta != c.meta || ra.k != rc.k) bad++;
+    Side sd;
+    make_side(f, sd);
+    const uint32_t men = sd.own & ~sd.ownK;
+    const uint32_t m01 = sd.turn ? sd.ownK : sd.own, m23 = sd.turn ? sd.own : sd.ownK;
+    const uint32_t J0 = m01 & sd.jd[0], J1 = m01 & sd.jd[1], J2 = m23 & sd.jd[2], J3 = m23 & sd.jd[3];
+    const uint32_t jall = sd.jd[0] | sd.jd[1] | sd.jd[2] | sd.jd[3];
+    const uint32_t jf = sd.turn ? (sd.jd[2] | sd.jd[3]) : (sd.jd[0] | sd.jd[1]);
+    const uint32_t lm = jump2<0>(J0 & men) | jump2<1>(J1 & men) | jump2<2>(J2 & men) | jump2<3>(J3 & men);
+    const uint32_t lk = jump2<0>(J0 & sd.ownK) | jump2<1>(J1 & sd.ownK) | jump2<2>(J2 & sd.ownK) |
+                        jump2<3>(J3 & sd.ownK);
+    if ((lm & jf) && !(lk & jall) && play_forced_men_multi(f, sd, J0, J1, J2, J3)) {
+      nf++;
+      if (nc != 1) bad++;  // the forced path claims a single move
+    }
+  }
+  if (forced) *forced = nf;
+  return bad;
+}
+
 long rh_eps_fast_matches_enum(uint64_t n, uint64_t seed) {
   uint64_t x = seed;
   auto next = [&]() {
