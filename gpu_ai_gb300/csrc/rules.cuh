@@ -730,6 +730,34 @@ GA_UNROLL
   return true;
 }
 
+// A capture ply where a king's capture can continue, with one first jump in
+// all and a chain that never forks, has exactly one legal move (about 70 % of
+// those plies in random play).  It is played here by following the chain with
+// the depth-first search's rules (capture_dirs: the position's jump masks, no
+// landing square twice in one sequence), as play_ply would play its only
+// move.  Returns false, with the board untouched, when there are two or more
+// moves or the chain reaches the depth limit (the search then reports it).
+GA_HD bool play_forced_king_chain(Board &b, const Side &s, uint32_t J0, uint32_t J1, uint32_t J2, uint32_t J3) {
+  if (popc(J0) + popc(J1) + popc(J2) + popc(J3) != 1) return false;
+  const int d0 = J0 ? 0 : (J1 ? 1 : (J2 ? 2 : 3));
+  const int from = ctz(J0 | J1 | J2 | J3);
+  if (!((s.ownK >> from) & 1u)) return false;  // only a king's chain is followed here
+  int t = from + jump_off(d0);
+  uint32_t removed = 1u << mid_square(from, t), visited = 1u << t;
+  for (int depth = 1;; depth++) {  // ends: each jump lands on a square not yet visited
+    const uint32_t rem = capture_dirs(s, t, true, visited);
+    if (rem == 0) break;
+    if ((rem & (rem - 1u)) != 0 || depth >= kMaxDepth) return false;
+    const int d = (int)((0x12131210u >> (2u * rem)) & 3u);  // the one direction left
+    const int nt = t + jump_off(d);
+    removed |= 1u << mid_square(t, nt);
+    visited |= 1u << nt;
+    t = nt;
+  }
+  apply_move(b, from, t, removed);
+  return true;
+}
+
 constexpr int kNeedMen = -2;   // a men's multi-jump ply was deferred
 constexpr int kNeedKing = -3;  // a ply where a king's capture can continue was deferred
 
@@ -772,6 +800,7 @@ GA_HD int play_ply_sched(Board &b, Pick &&pick, bool men_now, bool king_now) {
   const uint32_t cont_k = lk & jall, cont_m = lm & jf;
   if (cont_k | cont_m) {
     if (cont_k) {
+      if (play_forced_king_chain(b, s, J0, J1, J2, J3)) return 1;
       if (!king_now) return kNeedKing;
       return play_ply(b, pick);  // a king can continue: depth-first search with the cycle check
     }
@@ -1040,7 +1069,8 @@ GA_HD int play_ply_eps_sched(Board &b, Rng &rs, bool men_now, bool king_now) {
                       jump2<3>(J3 & s.ownK);
   const uint32_t cont_k = lk & jall, cont_m = lm & jf;
   if (cont_k | cont_m) {
-    if (!cont_k && play_forced_men_multi(b, s, J0, J1, J2, J3)) return 1;
+    if (cont_k ? play_forced_king_chain(b, s, J0, J1, J2, J3) : play_forced_men_multi(b, s, J0, J1, J2, J3))
+      return 1;
     if (cont_k && !king_now) return kNeedKing;
     if (!cont_k && !men_now) return kNeedMen;
     return ply_eps_greedy(b, rs);
@@ -1100,7 +1130,8 @@ GA_HD int play_ply_heur_sched(Board &b, Rng &rs, More &more, bool men_now, bool 
                       jump2<3>(J3 & s.ownK);
   const uint32_t cont_k = lk & jall, cont_m = lm & jf;
   if (cont_k | cont_m) {
-    if (!cont_k && play_forced_men_multi(b, s, J0, J1, J2, J3)) return 1;
+    if (cont_k ? play_forced_king_chain(b, s, J0, J1, J2, J3) : play_forced_men_multi(b, s, J0, J1, J2, J3))
+      return 1;
     if (cont_k && !king_now) return kNeedKing;
     if (!cont_k && !men_now) return kNeedMen;
     return ply_ref_heuristic(b, more);

@@ -133,10 +133,12 @@ extern "C" {
 // Returns the number of boards that differ.
 // play_ply_sched (every ply allowed) against the depth-first play_ply on n
 // pseudo-random boards: same move count, board and draws.  *forced counts the
-// boards whose ply was a men's multi-jump with one legal move, which
-// play_forced_men_multi plays without the men's tree.  Returns the number of
-// boards that differ.
-long rh_random_fast_matches_dfs(uint64_t n, uint64_t seed, uint64_t *forced) {
+// boards whose ply was a men's multi-jump with one legal move (played by
+// play_forced_men_multi without the men's tree), *forced_king those whose
+// ply was a king's continuing capture with one legal move (played by
+// play_forced_king_chain without the search).  Returns the number of boards
+// that differ.
+long rh_random_fast_matches_dfs(uint64_t n, uint64_t seed, uint64_t *forced, uint64_t *forced_king) {
   uint64_t x = seed;
   auto next = [&]() {
     uint64_t z = (x += 0x9E3779B97F4A7C15ull);
@@ -145,7 +147,7 @@ long rh_random_fast_matches_dfs(uint64_t n, uint64_t seed, uint64_t *forced) {
     return z ^ (z >> 31);
   };
   long bad = 0;
-  uint64_t nf = 0;
+  uint64_t nf = 0, nk = 0;
   for (uint64_t t = 0; t < n; t++) {
     uint32_t occ = (uint32_t)next() & (uint32_t)next();
     if (t & 1) occ |= (uint32_t)next() & (uint32_t)next();
@@ -174,9 +176,13 @@ long rh_random_fast_matches_dfs(uint64_t n, uint64_t seed, uint64_t *forced) {
     if ((lm & jf) && !(lk & jall) && play_forced_men_multi(f, sd, J0, J1, J2, J3)) {
       nf++;
       if (nc != 1) bad++;  // the forced path claims a single move
+    } else if ((lk & jall) && play_forced_king_chain(f, sd, J0, J1, J2, J3)) {
+      nk++;
+      if (nc != 1 || f.p1 != c.p1 || f.p2 != c.p2 || f.kings != c.kings || f.meta != c.meta) bad++;
     }
   }
   if (forced) *forced = nf;
+  if (forced_king) *forced_king = nk;
   return bad;
 }
 

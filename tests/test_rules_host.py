@@ -99,14 +99,15 @@ def test_buffered_draw_schedule_replays_on_oracle(rh, policy):
 
 def test_uniform_random_fast_ply_equals_depth_first_search(rh):
     """The uniform random ply the kernels play (branch-free common plies, the
-    men's tree, forced men's multi-jumps followed as a chain) plays the same
-    move with the same draws as the depth-first play_ply on 1 M random boards,
-    among them boards whose ply is a forced men's multi-jump."""
+    men's tree, forced men's multi-jumps and forced king captures followed as
+    a chain) plays the same move with the same draws as the depth-first
+    play_ply on 1 M random boards, among them boards of both forced kinds."""
     rh.rh_random_fast_matches_dfs.restype = ctypes.c_long
-    rh.rh_random_fast_matches_dfs.argtypes = [ctypes.c_uint64, ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64)]
-    forced = ctypes.c_uint64()
-    assert rh.rh_random_fast_matches_dfs(1_000_000, 23, ctypes.byref(forced)) == 0
-    assert forced.value > 1000
+    rh.rh_random_fast_matches_dfs.argtypes = [ctypes.c_uint64, ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64),
+                                              ctypes.POINTER(ctypes.c_uint64)]
+    forced, forced_king = ctypes.c_uint64(), ctypes.c_uint64()
+    assert rh.rh_random_fast_matches_dfs(1_000_000, 23, ctypes.byref(forced), ctypes.byref(forced_king)) == 0
+    assert forced.value > 1000 and forced_king.value > 1000
 
 
 def test_branch_free_eps_greedy_equals_enumeration(rh):
