@@ -772,6 +772,10 @@ constexpr int kNeedKing = -3;  // a ply where a king's capture can continue was 
 constexpr uint32_t kMenPeriod = 4, kMenPhase = 2;
 constexpr uint32_t kKingPeriod = 16, kKingPhase = 6;
 GA_HD constexpr uint32_t king_period(int policy) { return policy == 0 ? kKingPeriod : kKingPeriod / 2; }
+// a deferred ply must have a phase that comes round, or its game never ends
+static_assert((kMenPeriod & (kMenPeriod - 1u)) == 0 && kMenPhase < kMenPeriod, "men's phase outside its period");
+static_assert((kKingPeriod & (kKingPeriod - 1u)) == 0 && kKingPhase < kKingPeriod / 2,
+              "king phase outside the shorter king period");
 constexpr uint32_t kSparseLanes = 4;
 
 // One uniformly random ply, branch-free for direct moves and for captures
