@@ -89,11 +89,13 @@ __global__ void __launch_bounds__(BLOCK, (playout_min_blocks<POLICY, BLOCK>())) 
     // (policy 1, play_ply_heur_sched) takes two draws per legal move: its ply
     // loops over the moves for the warp's longest move list and refills the
     // ring every second step, so Philox still runs for the whole warp at once.
-    // Plies whose capture can be extended take longer code: men's multi-jumps
-    // (about 2.6% of plies) are deferred to every kMenPeriod-th iteration and
-    // plies where a king's capture can continue (about 0.7%, the costlier
-    // depth-first search) to every king_period(POLICY)-th, so that the lanes needing
-    // that code run it together and the other iterations stay branch-free.
+    // Plies whose capture can be extended take longer code.  Those with one
+    // legal move (about two thirds) follow their chain at once; the others,
+    // men's multi-jumps (about 1% of plies) and plies where a king's capture
+    // can continue (about 0.2%, the costlier depth-first search), are deferred
+    // to every kMenPeriod-th and every king_period(POLICY)-th iteration, so
+    // that the lanes needing that code run it together and the other
+    // iterations stay branch-free.
     // Once the work counter is exhausted, a warp with kSparseLanes or fewer
     // games defers nothing: its few games are latency-bound.
     //
