@@ -186,6 +186,27 @@ long rh_random_fast_matches_dfs(uint64_t n, uint64_t seed, uint64_t *forced, uin
   return bad;
 }
 
+// One uniform random ply of board b (p1, p2, kings, meta) played by the
+// kernels' play_ply_sched and by the depth-first play_ply on the same draws:
+// boards after the ply into fast_out / dfs_out, move counts into *n_fast /
+// *n_dfs.
+void rh_ply_fast_and_dfs(const uint32_t *b, uint64_t seed, uint32_t *fast_out, uint32_t *dfs_out, int *n_fast,
+                         int *n_dfs) {
+  Board a = load(b), c = load(b);
+  DrawRing ra, rc;
+  ra.start(seed, 0, 0);
+  rc.start(seed, 0, 0);
+  ra.refill();
+  rc.refill();
+  *n_fast = play_ply_sched(a, [&](uint32_t m) { return ra.pick(m); }, true, true);
+  *n_dfs = play_ply(c, [&](uint32_t m) { return rc.pick(m); });
+  const uint32_t fa[4] = {a.p1, a.p2, a.kings, a.meta}, fc[4] = {c.p1, c.p2, c.kings, c.meta};
+  for (int i = 0; i < 4; i++) {
+    fast_out[i] = fa[i];
+    dfs_out[i] = fc[i];
+  }
+}
+
 long rh_eps_fast_matches_enum(uint64_t n, uint64_t seed) {
   uint64_t x = seed;
   auto next = [&]() {

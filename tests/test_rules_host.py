@@ -110,6 +110,46 @@ def test_uniform_random_fast_ply_equals_depth_first_search(rh):
     assert forced.value > 1000 and forced_king.value > 1000
 
 
+def _sq(row, col):
+    """Dark square (row, col) -> bit index row*4 + col/2."""
+    assert (row + col) % 2 == 1
+    return row * 4 + col // 2
+
+
+def _bits(*cells):
+    return sum(1 << _sq(r, c) for r, c in cells)
+
+
+@pytest.mark.parametrize("name,board,n,after", [
+    # PLAYER_1 man (3,2) jumps (4,3) then (6,5), landing on the far row: forced, promotes
+    ("man_double_jump_promotes", (_bits((3, 2)), _bits((4, 3), (6, 5)), 0, 0), 1,
+     (_bits((7, 6)), 0, _bits((7, 6)), 1)),
+    # PLAYER_2 man (5,4) jumps (4,3) then (2,1): forced, no promotion on row 1
+    ("player2_man_double_jump", (_bits((4, 3), (2, 1)), _bits((5, 4)), 0, 1), 1,
+     (0, _bits((1, 0)), 0, 0)),
+    # PLAYER_1 king (2,1) jumps (3,2) then (5,4); it may not land on its start square again
+    ("king_double_jump", (_bits((2, 1)), _bits((3, 2), (5, 4)), _bits((2, 1)), 0), 1,
+     (_bits((6, 5)), 0, _bits((6, 5)), 1)),
+    # the man's chain forks after the first jump: two moves, not forced
+    ("man_chain_forks", (_bits((3, 2)), _bits((4, 3), (6, 5), (6, 3)), 0, 0), 2, None),
+])
+def test_capture_chains_on_crafted_boards(rh, name, board, n, after):
+    """Forced capture chains (one legal move) are played at once and equal the
+    depth-first search's move; a forking chain is left to the search."""
+    u32p, ip = ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(ctypes.c_int)
+    rh.rh_ply_fast_and_dfs.restype = None
+    rh.rh_ply_fast_and_dfs.argtypes = [u32p, ctypes.c_uint64, u32p, u32p, ip, ip]
+    b = np.array(board, dtype=np.uint32)
+    fast, dfs = np.zeros(4, np.uint32), np.zeros(4, np.uint32)
+    nf, nd = ctypes.c_int(), ctypes.c_int()
+    rh.rh_ply_fast_and_dfs(b.ctypes.data_as(u32p), 5, fast.ctypes.data_as(u32p), dfs.ctypes.data_as(u32p),
+                           ctypes.byref(nf), ctypes.byref(nd))
+    assert nf.value == nd.value == n, name
+    assert (fast == dfs).all(), name
+    if after is not None:
+        assert tuple(int(x) for x in fast) == after, name
+
+
 def test_branch_free_eps_greedy_equals_enumeration(rh):
     """The eps-greedy ply the kernels play without enumerating moves (best-move
     masks, bit-sliced jump gains) picks the same move with the same draws as
