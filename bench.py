@@ -301,6 +301,17 @@ def run_ours(args):
         eng.playouts_device(d_pos.data_ptr(), None, N_POS, REPS, TOTAL, 0x5EED, base + k * TOTAL, 0,
                             d_out.data_ptr(), sid)
 
+    bus = None
+    try:
+        bus = torch.cuda.get_device_properties(local).pci_bus_id if hasattr(
+            torch.cuda.get_device_properties(local), "pci_bus_id") else None
+    except Exception:
+        bus = None
+    # clocks are sampled from the warm-up on, through the timed loop, the
+    # end-to-end loop and the other policies' legs
+    sampler = ClockSampler(bus)
+    sampler.wait_first()
+    run0 = time.perf_counter()
     for k in range(args.warmup):
         flush.zero_()
         step(k)
@@ -309,18 +320,10 @@ def run_ours(args):
     if st:
         raise RuntimeError(f"kernel status {st}")
 
-    bus = None
-    try:
-        bus = torch.cuda.get_device_properties(local).pci_bus_id if hasattr(
-            torch.cuda.get_device_properties(local), "pci_bus_id") else None
-    except Exception:
-        bus = None
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     plies = 0
     barrier(world)
     torch.cuda.synchronize()
-    sampler = ClockSampler(bus)
-    sampler.wait_first()
     wall0 = time.perf_counter()
     for k in range(args.steps):
         flush.zero_()
@@ -335,7 +338,6 @@ def run_ours(args):
     wall1 = time.perf_counter()
     wall = wall1 - wall0
     barrier(world)
-    clocks = sampler.stop(wall0, wall1)
     kern_s = sum(a.elapsed_time(b) for a, b in ev) / 1e3
     kern_s_max = max_over_ranks(kern_s, world)
     value = world * args.steps * TOTAL / kern_s_max
@@ -353,6 +355,8 @@ def run_ours(args):
     for k in range(args.steps):
         eng.playouts(positions, reps, seed=0xE2E, stream_base=base + (k + 2) * TOTAL, out=out)
     e2e_s = time.perf_counter() - t0
+    if rank != 0:
+        sampler.stop()
     e2e_s = max_over_ranks(e2e_s, world)
     assert out.shape == (TOTAL,)
     e2e = {"value": world * args.steps * TOTAL / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
@@ -363,6 +367,7 @@ def run_ours(args):
     peaks, src = measured_peaks()
     sm_mhz = float(peaks.get("sm_max_mhz", 2070.0))
     peak_ops = info["sms"] * 128 * sm_mhz * 1e6  # lanes issued per second: SMs x 4 schedulers x 32 lanes
+    clocks = summarize_clocks(sampler.rows, wall0, wall1)  # the timed loop
     plies_s = plies / kern_s
     roof = {"bound": "int_issue", "unit": "Tlane-op/s",
             "peak": peak_ops / 1e12, "peak_source": f"{info['sms']} SMs x 128 lanes x {sm_mhz:.0f} MHz ({src})",
@@ -371,8 +376,6 @@ def run_ours(args):
     if OPS_PER_PLY:
         roof["achieved"] = plies_s * OPS_PER_PLY / 1e12
         roof["frac"] = roof["achieved"] / roof["peak"]
-        if clocks.get("sm_mhz"):
-            roof["frac_at_sampled_clock"] = roof["frac"] * sm_mhz / clocks["sm_mhz"]
     else:
         roof["achieved"] = None
         roof["frac"] = None
@@ -409,6 +412,17 @@ def run_ours(args):
         pols[name] = {"playouts_per_s": len(ts) * TOTAL / sum(ts), "ms_per_step": sum(ts) / len(ts) * 1e3,
                       "plies_per_playout": pl_sum / (len(ts) * TOTAL)}
     line["policies"] = pols
+    # a short timed loop can fall between two 50 ms samples: then the clocks
+    # of the whole GPU run (warm-up, timed loops, policy legs) are reported
+    run1 = time.perf_counter()
+    whole = sampler.stop(run0, run1)
+    if (clocks.get("samples") or 0) < 3:
+        clocks = dict(whole, window="warm-up to the end of the policy legs (timed loop shorter than 3 samples)")
+    else:
+        clocks["window"] = "timed loop"
+    line["clocks"] = clocks
+    if roof.get("frac") and clocks.get("sm_mhz"):
+        roof["frac_at_sampled_clock"] = roof["frac"] * sm_mhz / clocks["sm_mhz"]
     if world == 1 and not args.no_cpu:
         line["cpu_baseline"] = time_cpu_baseline(positions)
         pols["ref_heuristic"]["cpu_baseline"] = time_cpu_heuristic(positions)

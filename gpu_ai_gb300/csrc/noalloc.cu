@@ -32,12 +32,20 @@ static __device__ __align__(256) uint32_t g_scratch[kScratchWords];
 
 constexpr int kMaxDevices = 64;
 
+// Threads per block for each policy: the uniform random policy runs in
+// 512-thread blocks, the others in 256-thread blocks (the allocating entry
+// point's default launch shapes).
+constexpr int kBlock[3] = {2 * ga::kPlayoutBlock, ga::kPlayoutBlock, ga::kPlayoutBlock};
+
 struct DeviceState {
   std::atomic<bool> ready{false};
   uint32_t *scratch = nullptr;  // device address of g_scratch on this device
   int sms = 0;
   int blocks_per_sm[3] = {0, 0, 0};
-  std::mutex call;  // one call at a time per device: calls share g_scratch
+  std::mutex call;  // one call at a time per device: calls share g_scratch and `offsets`
+  // host staging of the repetition prefix sums (static storage: untouched
+  // pages cost nothing until a device's first call with repetitions)
+  uint32_t offsets[kMaxPositions + 1];
 };
 
 DeviceState g_dev[kMaxDevices];
@@ -61,7 +69,7 @@ int setup(int dev, DeviceState &d) {
   e = cudaDeviceGetAttribute(&d.sms, cudaDevAttrMultiProcessorCount, dev);
   if (e != cudaSuccess) return cuda_error(e, "cudaDeviceGetAttribute");
   for (int policy = 0; policy < 3; policy++) {
-    e = ga::playout_occupancy(policy, ga::kPlayoutBlock, &d.blocks_per_sm[policy]);
+    e = ga::playout_occupancy(policy, kBlock[policy], &d.blocks_per_sm[policy]);
     if (e != cudaSuccess) return cuda_error(e, "occupancy query");
     if (d.blocks_per_sm[policy] < 1) d.blocks_per_sm[policy] = 1;
   }
@@ -109,21 +117,16 @@ extern "C" int gpuai_playouts_noalloc(const gpuai_board *d_pos, const uint32_t *
   uint32_t *scratch = d.scratch;
   uint32_t *offsets = nullptr;
   if (reps) {
-    // prefix sums staged through a small stack buffer, 256 entries per copy
+    // all npos+1 prefix sums staged in the device's static host array, one copy
     offsets = scratch + kOffsetsWord;
-    uint32_t chunk[256];
     uint32_t acc = 0;
-    for (uint32_t base = 0; base <= npos; base += 256) {
-      const uint32_t cnt = (npos + 1 - base) < 256u ? (npos + 1 - base) : 256u;
-      for (uint32_t q = 0; q < cnt; q++) {
-        chunk[q] = acc;
-        if (base + q < npos) acc += reps[base + q];
-      }
-      e = cudaMemcpyAsync(offsets + base, chunk, cnt * sizeof(uint32_t), cudaMemcpyHostToDevice, s);
-      if (e != cudaSuccess) return cuda_error(e, "copy of the repetition prefix sums");
-      e = cudaStreamSynchronize(s);  // the stack buffer is reused for the next chunk
-      if (e != cudaSuccess) return cuda_error(e, "copy of the repetition prefix sums");
+    for (uint32_t p = 0; p < npos; p++) {
+      d.offsets[p] = acc;
+      acc += reps[p];
     }
+    d.offsets[npos] = acc;
+    e = cudaMemcpyAsync(offsets, d.offsets, (npos + 1) * sizeof(uint32_t), cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) return cuda_error(e, "copy of the repetition prefix sums");
   }
   // the counter, status and ply count keep the previous call's values: clear them
   e = cudaMemsetAsync(scratch, 0, 4 * sizeof(uint32_t), s);
@@ -141,9 +144,9 @@ extern "C" int gpuai_playouts_noalloc(const gpuai_board *d_pos, const uint32_t *
   a.status = scratch + 1;
   a.plies = reinterpret_cast<unsigned long long *>(scratch + 2);
   const long long resident = (long long)d.sms * d.blocks_per_sm[policy];
-  const long long need = ((long long)total + ga::kPlayoutBlock - 1) / ga::kPlayoutBlock;
+  const long long need = ((long long)total + kBlock[policy] - 1) / kBlock[policy];
   const int grid = (int)(need < resident ? need : resident);
-  e = ga::launch_playouts(a, policy, ga::kPlayoutBlock, grid, s);
+  e = ga::launch_playouts(a, policy, kBlock[policy], grid, s);
   if (e != cudaSuccess) return cuda_error(e, "playout kernel launch");
   uint32_t status = 0;
   e = cudaMemcpyAsync(&status, scratch + 1, sizeof status, cudaMemcpyDeviceToHost, s);

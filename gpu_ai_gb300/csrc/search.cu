@@ -37,6 +37,7 @@
 // the node, w = score in half points of the player who moved into the node.
 #include "../../include/gpuai.h"
 #include "host/state.hpp"
+#include "detmath.cuh"
 #include "launch.h"
 #include "net.h"
 #include "rules.cuh"
@@ -191,24 +192,31 @@ __device__ void expand_at(const Pool &p, int32_t n, int32_t base, int k) {
 // proportion to UCB1 weights rounded down; the remainder goes one each to the
 // heaviest children (first on ties).  Weights that sum to zero count as
 // equal.  Fills give[0..k) and returns the number of children given slots.
+// The weights use the correctly rounded operations of detmath.cuh in a fixed
+// order, so the CPU restatement (oracle/search.py) reproduces every split.
+__device__ __forceinline__ float ucb_weight(uint4 ci, float lnN) {
+  const float mean = dm::div(dm::mul(0.5f, (float)ci.w), (float)ci.z);
+  return dm::add(mean, dm::mul(kUcbC, dm::sqrt_(dm::div(lnN, (float)ci.z))));
+}
+
 __device__ int split_slots(const Pool &p, int32_t first, int k, uint32_t parent_visits, uint32_t T,
                            uint32_t *give) {
-  const float lnN = logf((float)(parent_visits > 0 ? parent_visits : 1u));
+  const float lnN = dm::det_log((float)(parent_visits > 0 ? parent_visits : 1u));
   float wsum = 0.0f;
   int untried = 0;
   for (int c = 0; c < k; c++) {
     const uint4 ci = p.info[first + c];
     if (ci.z == 0) untried++;
-    else wsum += 0.5f * (float)ci.w / (float)ci.z + kUcbC * sqrtf(lnN / (float)ci.z);
+    else wsum = dm::add(wsum, ucb_weight(ci, lnN));
   }
   const bool equal = untried == 0 && !(wsum > 0.0f);
   uint32_t assigned = 0;
   float w[kMaxChildren];
   for (int c = 0; c < k; c++) {
     const uint4 ci = p.info[first + c];
-    w[c] = ci.z == 0 ? 3.0e38f : (equal ? 1.0f : 0.5f * (float)ci.w / (float)ci.z + kUcbC * sqrtf(lnN / (float)ci.z));
+    w[c] = ci.z == 0 ? 3.0e38f : (equal ? 1.0f : ucb_weight(ci, lnN));
     if (untried > 0) give[c] = ci.z == 0 ? T / (uint32_t)untried : 0u;
-    else give[c] = (uint32_t)((float)T * (w[c] / (equal ? (float)k : wsum)));
+    else give[c] = (uint32_t)dm::mul((float)T, dm::div(w[c], equal ? (float)k : wsum));
     assigned += give[c];
   }
   uint64_t extra = 0;  // children that already took one of the remaining slots
@@ -241,32 +249,35 @@ __device__ int split_puct(const Pool &p, int32_t n, int32_t first, int k, uint32
                           uint32_t parent_score2, uint32_t st, uint32_t T, float c_puct, uint32_t *give) {
   float q[kMaxChildren], u[kMaxChildren], pr[kMaxChildren], nv[kMaxChildren];
   const bool priors = (st & kEvaluated) && k <= (int)kPriors;
-  const float fpu = parent_visits ? fmaxf(0.0f, 1.0f - 0.5f * (float)parent_score2 / (float)parent_visits -
-                                                    kFpuReduction)
-                                  : 0.5f;
+  const float fpu =
+      parent_visits
+          ? fmaxf(0.0f, dm::sub(dm::sub(1.0f, dm::div(dm::mul(0.5f, (float)parent_score2), (float)parent_visits)),
+                                kFpuReduction))
+          : 0.5f;
+  const float uniform = dm::div(1.0f, (float)k);
   for (int c = 0; c < k; c++) {
     const uint4 ci = p.info[first + c];
-    q[c] = ci.z ? 0.5f * (float)ci.w / (float)ci.z : fpu;
-    nv[c] = 1.0f + (float)(ci.z / kUnits);
-    pr[c] = c_puct * (priors ? __half2float(p.prior[(size_t)n * kPriors + c]) : 1.0f / (float)k);
-    u[c] = pr[c] / nv[c];  // exploration term without the sqrt(N) factor
+    q[c] = ci.z ? dm::div(dm::mul(0.5f, (float)ci.w), (float)ci.z) : fpu;
+    nv[c] = dm::add(1.0f, (float)(ci.z / kUnits));
+    pr[c] = dm::mul(c_puct, priors ? __half2float(p.prior[(size_t)n * kPriors + c]) : uniform);
+    u[c] = dm::div(pr[c], nv[c]);  // exploration term without the sqrt(N) factor
     give[c] = 0;
   }
   const float N = (float)(parent_visits / kUnits);
   for (uint32_t t = 0; t < T; t++) {
-    const float sq = sqrtf(N + (float)t + 1.0f);
+    const float sq = dm::sqrt_(dm::add(dm::add(N, (float)t), 1.0f));
     int best = 0;
     float bs = -3.0e38f;
     for (int c = 0; c < k; c++) {
-      const float sc = fmaf(sq, u[c], q[c]);
+      const float sc = dm::add(dm::mul(sq, u[c]), q[c]);
       if (sc > bs) {
         bs = sc;
         best = c;
       }
     }
     give[best]++;
-    nv[best] += 1.0f;
-    u[best] = pr[best] / nv[best];
+    nv[best] = dm::add(nv[best], 1.0f);
+    u[best] = dm::div(pr[best], nv[best]);
   }
   int kids = 0;
   for (int c = 0; c < k; c++) kids += give[c] != 0;
@@ -437,15 +448,15 @@ __global__ void backprop_learned_kernel(Pool p, Table t, Leaves l, uint32_t ppl,
   const int32_t leaf = l.node[i];
   int sum = 0;  // outcomes for PLAYER_1
   for (uint32_t k = 0; k < ppl; k++) sum += l.out[(size_t)i * ppl + k];
-  const float pm = (float)sum / (float)ppl;
+  const float pm = dm::div((float)sum, (float)ppl);
   float x1 = pm;
   const float v = l.value[i];
   if (v <= 1.0f) {  // kTerminalLeaf (> 1): a finished game, whose playouts give the exact result
     const float v1 = (p.board[leaf].w & 1u) ? -v : v;  // the value is for the side to move
-    x1 = lrn.value_weight * v1 + (1.0f - lrn.value_weight) * pm;
+    x1 = dm::add(dm::mul(lrn.value_weight, v1), dm::mul(dm::sub(1.0f, lrn.value_weight), pm));
   }
   x1 = fminf(1.0f, fmaxf(-1.0f, x1));
-  const uint32_t s1 = (uint32_t)lrintf((float)kUnits * (1.0f + x1));  // half points of PLAYER_1
+  const uint32_t s1 = (uint32_t)__float2int_rn(dm::mul((float)kUnits, dm::add(1.0f, x1)));  // half points of PLAYER_1
   const uint32_t s2 = 2u * kUnits - s1;
   for (int32_t n = leaf; n >= 0; n = p.parent[n]) {
     const uint32_t mover = (p.board[n].w & 1u) ^ 1u;  // 0: PLAYER_1 moved into n
@@ -471,7 +482,7 @@ __global__ void leaf_eval_kernel(Pool p, Leaves l, const __nv_bfloat16 *logits, 
   const uint32_t J = jumpers(sd);
   const int k = count_moves(sd, J);
   const bool over = k == 0 || ((b.meta >> 8) & 0xffu) >= (uint32_t)kDrawPlies;
-  l.value[i] = over ? kTerminalLeaf : tanhf(vraw[i]);
+  l.value[i] = over ? kTerminalLeaf : dm::det_tanh(vraw[i]);
   const int32_t n = l.node[i];
   const uint32_t st = p.info[n].y >> 16;
   if (over || (st & (kEvaluated | kTerminal))) return;
@@ -501,10 +512,11 @@ __global__ void leaf_eval_kernel(Pool p, Leaves l, const __nv_bfloat16 *logits, 
       lmax = fmaxf(lmax, lg[u]);
     }
     float sum = 0.0f;
-    for (int u = 0; u < np; u++) sum += expf(lg[u] - lmax);
+    for (int u = 0; u < np; u++) sum = dm::add(sum, dm::det_exp(dm::sub(lg[u], lmax)));
     for (int j = 0; j < k; j++) {
       const int u = of[j];
-      p.prior[(size_t)n * kPriors + j] = __float2half(expf(lg[u] - lmax) / sum / (float)mult[u]);
+      p.prior[(size_t)n * kPriors + j] =
+          __float2half_rn(dm::div(dm::div(dm::det_exp(dm::sub(lg[u], lmax)), sum), (float)mult[u]));
     }
   }
   atomicOr(&p.info[n].y, kEvaluated << 16);
@@ -895,6 +907,83 @@ int gpuai_searches_children(gpuai_searches *s, int32_t slot, gpuai_move *moves, 
     if (visits) visits[i] = v[i];
     if (score2) score2[i] = sc[i];
     if (moves && i < all.size()) moves[i] = all[i];
+  }
+  return GPUAI_OK;
+}
+
+int gpuai_searches_nodes(gpuai_searches *s, int32_t slot, uint32_t max_nodes, uint32_t *info, gpuai_board *boards,
+                         int32_t *parent, uint16_t *priors, uint32_t *nnodes) {
+  if (!s || !nnodes) return err(GPUAI_ERR_INVALID, "gpuai_searches_nodes: NULL");
+  std::lock_guard<std::mutex> lock(s->mu);
+  if (slot < 0 || (uint32_t)slot >= s->slots || s->start[slot] < 0)
+    return err(GPUAI_ERR_INVALID, "gpuai_searches_nodes: no such search");
+  if (priors && !s->pool.prior) return err(GPUAI_ERR_INVALID, "gpuai_searches_nodes: the searches keep no priors");
+  SCK(cudaSetDevice(s->device), "cudaSetDevice");
+  const int32_t r = s->start[slot];
+  int32_t next = 0;
+  SCK(cudaMemcpyAsync(&next, s->tab.node_next + slot, 4, cudaMemcpyDeviceToHost, s->stream), "nodes");
+  SCK(cudaStreamSynchronize(s->stream), "nodes");
+  const uint32_t used = (uint32_t)(next - r);
+  *nnodes = used;
+  const uint32_t n = used < max_nodes ? used : max_nodes;
+  if (n == 0) return GPUAI_OK;
+  std::vector<uint4> inf(n);
+  std::vector<int32_t> par(n);
+  SCK(cudaMemcpyAsync(inf.data(), s->pool.info + r, 16 * (size_t)n, cudaMemcpyDeviceToHost, s->stream), "nodes");
+  SCK(cudaMemcpyAsync(par.data(), s->pool.parent + r, 4 * (size_t)n, cudaMemcpyDeviceToHost, s->stream), "nodes");
+  if (boards)
+    SCK(cudaMemcpyAsync(boards, s->pool.board + r, 16 * (size_t)n, cudaMemcpyDeviceToHost, s->stream), "nodes");
+  if (priors)
+    SCK(cudaMemcpyAsync(priors, s->pool.prior + (size_t)r * kPriors, 2 * kPriors * (size_t)n,
+                        cudaMemcpyDeviceToHost, s->stream),
+        "nodes");
+  SCK(cudaStreamSynchronize(s->stream), "nodes");
+  for (uint32_t i = 0; i < n; i++) {
+    if (info) {
+      info[4 * i] = inf[i].x == 0xffffffffu ? 0xffffffffu : inf[i].x - (uint32_t)r;
+      info[4 * i + 1] = inf[i].y;
+      info[4 * i + 2] = inf[i].z;
+      info[4 * i + 3] = inf[i].w;
+    }
+    if (parent) parent[i] = par[i] < 0 ? -1 : par[i] - r;
+  }
+  return GPUAI_OK;
+}
+
+int gpuai_searches_leaves(gpuai_searches *s, uint32_t max_leaves, uint32_t *nleaves, int32_t *search, int32_t *node,
+                          gpuai_board *boards, uint64_t *streams, int8_t *outcomes, float *net_value,
+                          uint16_t *net_logits) {
+  if (!s || !nleaves) return err(GPUAI_ERR_INVALID, "gpuai_searches_leaves: NULL");
+  std::lock_guard<std::mutex> lock(s->mu);
+  if ((net_value || net_logits) && !s->net)
+    return err(GPUAI_ERR_INVALID, "gpuai_searches_leaves: no network is attached");
+  SCK(cudaSetDevice(s->device), "cudaSetDevice");
+  uint32_t sizes[2] = {0, 0};
+  SCK(cudaMemcpyAsync(sizes, s->leaves.sizes, 8, cudaMemcpyDeviceToHost, s->stream), "leaves");
+  SCK(cudaStreamSynchronize(s->stream), "leaves");
+  *nleaves = sizes[0];
+  const uint32_t n = sizes[0] < max_leaves ? sizes[0] : max_leaves;
+  if (n == 0) return GPUAI_OK;
+  std::vector<int32_t> srch(n), nd(n);
+  SCK(cudaMemcpyAsync(srch.data(), s->leaves.search, 4 * (size_t)n, cudaMemcpyDeviceToHost, s->stream), "leaves");
+  SCK(cudaMemcpyAsync(nd.data(), s->leaves.node, 4 * (size_t)n, cudaMemcpyDeviceToHost, s->stream), "leaves");
+  if (boards)
+    SCK(cudaMemcpyAsync(boards, s->leaves.board, 16 * (size_t)n, cudaMemcpyDeviceToHost, s->stream), "leaves");
+  if (streams)
+    SCK(cudaMemcpyAsync(streams, s->leaves.stream, 8 * (size_t)n, cudaMemcpyDeviceToHost, s->stream), "leaves");
+  if (outcomes)
+    SCK(cudaMemcpyAsync(outcomes, s->leaves.out, (size_t)n * s->ppl, cudaMemcpyDeviceToHost, s->stream), "leaves");
+  if (net_value)
+    SCK(cudaMemcpyAsync(net_value, s->fw.vraw, 4 * (size_t)n, cudaMemcpyDeviceToHost, s->stream), "leaves");
+  if (net_logits)
+    SCK(cudaMemcpyAsync(net_logits, s->fw.logits_b, 2 * (size_t)n * ga::net::kOut, cudaMemcpyDeviceToHost,
+                        s->stream),
+        "leaves");
+  SCK(cudaStreamSynchronize(s->stream), "leaves");
+  for (uint32_t i = 0; i < n; i++) {
+    if (search) search[i] = srch[i];
+    const int32_t st = (srch[i] >= 0 && (uint32_t)srch[i] < s->slots) ? s->start[srch[i]] : -1;
+    if (node) node[i] = st < 0 ? -1 : nd[i] - st;
   }
   return GPUAI_OK;
 }

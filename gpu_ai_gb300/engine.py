@@ -118,6 +118,8 @@ def load_library(path: str = LIB_PATH):
     lib.gpuai_set_layout.argtypes = [vp, ctypes.c_int32, ctypes.c_int32]
     lib.gpuai_get_layout.argtypes = [vp, ctypes.c_int32, _i32p]
     lib.gpuai_searches_set_net.argtypes = [vp, vp, ctypes.c_float, ctypes.c_float]
+    lib.gpuai_searches_nodes.argtypes = [vp, ctypes.c_int32, ctypes.c_uint32, vp, vp, vp, vp, _u32p]
+    lib.gpuai_searches_leaves.argtypes = [vp, ctypes.c_uint32, _u32p, vp, vp, vp, vp, vp, vp, vp]
     for name in header_symbols():
         if name not in ("gpuai_last_error", "gpuai_destroy", "gpuai_searches_destroy", "gpuai_net_destroy"):
             getattr(lib, name).restype = ctypes.c_int
@@ -271,6 +273,7 @@ class Searches:
                                               playouts_per_leaf, policy, seed, ctypes.byref(h)))
         self.h = h
         self.max_searches = max_searches
+        self.ppl = playouts_per_leaf
 
     def close(self):
         if self.h:
@@ -329,6 +332,50 @@ class Searches:
         """Evaluate leaves with `net` (None: plain playout searches)."""
         _check(self.lib.gpuai_searches_set_net(self.h, net.h if net is not None else None, value_weight, c_puct))
         self.net = net  # keep the network alive while the searches use it
+
+    def nodes(self, slot: int, priors: bool = False):
+        """The search's tree, nodes numbered from its root: info (n, 4) = {first
+        child (0xFFFFFFFF before expansion), children | state << 16, visits,
+        score2}, boards (n, 4), parent (n,), and priors (n, 32) FP16 when asked."""
+        n = ctypes.c_uint32()
+        _check(self.lib.gpuai_searches_nodes(self.h, slot, 0, None, None, None, None, ctypes.byref(n)))
+        k = n.value
+        info = np.zeros((k, 4), np.uint32)
+        boards = np.zeros((k, 4), np.uint32)
+        parent = np.zeros(k, np.int32)
+        pri = np.zeros((k, 32), np.uint16) if priors else None
+        _check(self.lib.gpuai_searches_nodes(self.h, slot, k, info.ctypes.data, boards.ctypes.data,
+                                             parent.ctypes.data, pri.ctypes.data if priors else None,
+                                             ctypes.byref(n)))
+        out = {"info": info, "boards": boards, "parent": parent}
+        if priors:
+            out["priors"] = pri.view(np.float16)
+        return out
+
+    def leaves(self, net: bool = False):
+        """The last step's leaf slots: search, node (from the search's root),
+        boards, first stream id, outcomes (n, playouts_per_leaf) and, with
+        net, the raw value output and the (n, 1024) logits as float32
+        (playouts_per_leaf outcomes per slot)."""
+        n = ctypes.c_uint32()
+        _check(self.lib.gpuai_searches_leaves(self.h, 0, ctypes.byref(n), None, None, None, None, None, None, None))
+        k = n.value
+        search = np.zeros(k, np.int32)
+        node = np.zeros(k, np.int32)
+        boards = np.zeros((k, 4), np.uint32)
+        streams = np.zeros(k, np.uint64)
+        outcomes = np.zeros((k, self.ppl), np.int8)
+        value = np.zeros(k, np.float32) if net else None
+        logits = np.zeros((k, NET_LOGITS), np.uint16) if net else None
+        _check(self.lib.gpuai_searches_leaves(self.h, k, ctypes.byref(n), search.ctypes.data, node.ctypes.data,
+                                              boards.ctypes.data, streams.ctypes.data, outcomes.ctypes.data,
+                                              value.ctypes.data if net else None,
+                                              logits.ctypes.data if net else None))
+        out = {"search": search, "node": node, "boards": boards, "streams": streams, "outcomes": outcomes}
+        if net:
+            out["net_value"] = value
+            out["net_logits"] = (logits.astype(np.uint32) << 16).view(np.float32)
+        return out
 
     def best(self, slot: int):
         """Most visited root move (None for a finished game) and the child statistics."""

@@ -171,6 +171,29 @@ int gpuai_searches_poll(gpuai_searches *s, uint64_t *done, uint64_t *budget, uin
 int gpuai_searches_children(gpuai_searches *s, int32_t slot, gpuai_move *moves, uint32_t *visits,
                             uint32_t *score2, uint32_t max_children, uint32_t *nchildren, uint32_t *nodes_used);
 
+/* Inspection of the device trees, for tests and tools (no counterpart in the
+ * reference, whose GameTree keeps its nodes private).  Synchronise first.
+ * gpuai_searches_nodes: the first min(nnodes, max_nodes) nodes of the search in
+ * `slot`, numbered from its root (0) in allocation order; *nnodes = nodes in
+ * use.  info (optional, 4 words per node): first child (0xFFFFFFFF before
+ * expansion), children | state bits << 16 (1 expanded, 2 finished root,
+ * 4 evaluated by the network), playouts through the node (visit units for
+ * learned searches), score in half points of the player who moved into the
+ * node.  boards, parent (-1 for the root) and priors (32 FP16 bit patterns
+ * per node, learned searches only) are optional too. */
+int gpuai_searches_nodes(gpuai_searches *s, int32_t slot, uint32_t max_nodes, uint32_t *info, gpuai_board *boards,
+                         int32_t *parent, uint16_t *priors, uint32_t *nnodes);
+/* The last step's leaf slots, in slot order (searches in slot order, each
+ * search's slots in the order its selection emitted them); *nleaves = their
+ * number.  Per slot (all optional): search slot, node (numbered from the
+ * search's root), board, first random-stream id (its playouts use that id and
+ * the next playouts_per_leaf - 1), outcomes (playouts_per_leaf int8 each) and,
+ * with a network attached, its raw value output (before tanh) and 1024 BF16
+ * move logits (bit patterns). */
+int gpuai_searches_leaves(gpuai_searches *s, uint32_t max_leaves, uint32_t *nleaves, int32_t *search, int32_t *node,
+                          gpuai_board *boards, uint64_t *streams, int8_t *outcomes, float *net_value,
+                          uint16_t *net_logits);
+
 /* ---- policy/value network ----
  * No counterpart in the reference (its only evaluation is the material
  * heuristic, src/heuristic.cu:20-49).  A BF16 MLP on the tensor cores with FP32
@@ -254,11 +277,12 @@ int gpuai_searches_set_net(gpuai_searches *s, gpuai_net *net, float value_weight
  * held until the process exits); larger npos is rejected with
  * GPUAI_ERR_INVALID.  No context is needed: the call runs on the current
  * device and `stream` (NULL: the legacy default stream) and returns after the
- * playouts finished.  The first call on a device looks up that array's device
- * address; make that first call before any stream capture.  All calls share
- * the array, which keeps the previous call's contents (the call clears what
- * must start at zero); calls on one device are serialised by the library,
- * and launches that overlapped on the GPU would race on it. */
+ * playouts finished: every call synchronises `stream` before it returns.  The
+ * first call on a device looks up that array's device address; make that
+ * first call before any stream capture.  All calls share the array,
+ * which keeps the previous call's contents (the call clears what must start
+ * at zero); calls on one device are serialised by the library, and launches
+ * that overlapped on the GPU would race on it. */
 #define GPUAI_NOALLOC_MAX_POSITIONS 16384
 int gpuai_playouts_noalloc(const gpuai_board *d_pos, const uint32_t *reps, uint32_t npos,
                            uint64_t seed, uint64_t stream_base, int32_t policy, int8_t *d_out,

@@ -18,7 +18,8 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 ORACLE_DIR = os.path.join(ROOT, "oracle")
 ORACLE_SO = os.path.join(ORACLE_DIR, "_build", "liboracle.so")
 REF_SO = os.path.join(ORACLE_DIR, "_ref", "libref.so")
-REF_SRC = "/root/reference/src"
+# the reference's sources, where present (GPUAI_REFERENCE_SRC overrides)
+REF_SRC = os.environ.get("GPUAI_REFERENCE_SRC", "/root/reference/src")
 
 _u32p = ctypes.POINTER(ctypes.c_uint32)
 _u8p = ctypes.POINTER(ctypes.c_uint8)
@@ -36,7 +37,7 @@ def build_ref() -> bool:
     """Compile the reference's host code from its sources, where present."""
     if not os.path.isdir(REF_SRC):
         return False
-    subprocess.run(["make", "-s", "-j8", "-C", ORACLE_DIR, "ref"], check=True,
+    subprocess.run(["make", "-s", "-j8", "-C", ORACLE_DIR, "ref", "REF_SRC=" + REF_SRC], check=True,
                    stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
     return os.path.exists(REF_SO)
 
@@ -108,6 +109,48 @@ def genmoves(pos: np.ndarray, max_moves: int = 128, lib=None):
     if rc != 0:
         raise RuntimeError("move list overflow")
     return out, counts
+
+
+_children_cache: dict = {}
+
+
+def children(board):
+    """(child boards (k, 4), packed moves (k, 32)) of one board in move-list
+    order, by the restatement's genMoves and State::move (memoised)."""
+    key = tuple(int(v) for v in board)
+    hit = _children_cache.get(key)
+    if hit is not None:
+        return hit
+    pos = np.array([key], dtype=np.uint32)
+    mv, cnt = genmoves(pos, max_moves=128)
+    k = int(cnt[0])
+    moves = np.ascontiguousarray(mv[0, :k])
+    boards = np.repeat(pos, k, axis=0)
+    lib = oracle()
+    for i in range(k):
+        row = np.ascontiguousarray(boards[i])
+        if lib.or_apply_packed_b16(_ptr(row, _u32p), _ptr(np.ascontiguousarray(moves[i]), _u8p)) != 0:
+            raise RuntimeError("apply failed")
+        boards[i] = row
+    if len(_children_cache) > 1_000_000:
+        _children_cache.clear()
+    _children_cache[key] = (boards, moves)
+    return boards, moves
+
+
+def fake_outcome(board, salt: int) -> int:
+    """The deterministic stand-in for a playout of tests/host_tree.cpp and
+    oracle/ref_shim.cpp: +1 (PLAYER_1), -1 (PLAYER_2) or 0 from a hash of the board."""
+    m = (1 << 64) - 1
+    b = [int(v) for v in board]
+    x = ((b[0] | (b[1] << 32)) ^ ((b[2] * 0x9E3779B97F4A7C15) & m) ^ ((b[3] * 0xC2B2AE3D27D4EB4F) & m) ^ salt) & m
+    x ^= x >> 31
+    x = (x * 0x7FB5D329728EA185) & m
+    x ^= x >> 27
+    x = (x * 0x81DADEF4BC2DD44D) & m
+    x ^= x >> 33
+    r = x % 7
+    return 1 if r < 3 else (-1 if r < 6 else 0)
 
 
 def canonical_moves(out: np.ndarray, counts: np.ndarray):

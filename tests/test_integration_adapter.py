@@ -1,4 +1,5 @@
-"""The PlayoutDriver adapter that INTEGRATION.md gives a maintainer compiles
+"""The PlayoutDriver adapter a maintainer adds to the reference
+(include/adapters/gpuPlayout.cpp) compiles
 against the reference's own headers (src/playout.hpp:27-33,
 src/state.hpp), converts the reference's starting State to the engine's
 start board, and reports a missing GPU as std::runtime_error instead of
@@ -33,12 +34,7 @@ int main() {
 '''
 
 
-def _adapter_source():
-    text = open(os.path.join(ROOT, "INTEGRATION.md")).read()
-    blocks = re.findall(r"```cpp\n(.*?)```", text, flags=re.S)
-    src = [b for b in blocks if "class GpuPlayoutDriver" in b]
-    assert len(src) == 1
-    return src[0]
+ADAPTER = os.path.join(ROOT, "include", "adapters", "gpuPlayout.cpp")
 
 
 @pytest.fixture(scope="module")
@@ -50,8 +46,7 @@ def adapter_exe(tmp_path_factory):
     if not os.path.exists(os.path.join(LIB, "libgpuai.so")):
         pytest.skip("libgpuai.so not built")
     d = tmp_path_factory.mktemp("adapter")
-    (d / "gpuPlayout.cpp").write_text(_adapter_source())
-    (d / "main.cpp").write_text('#include "gpuPlayout.cpp"\n' + MAIN)
+    (d / "main.cpp").write_text('#include "' + ADAPTER + '"\n' + MAIN)
     exe = d / "adapter"
     ref_dir = os.path.dirname(L.REF_SO)
     subprocess.run(["g++", "-std=c++17", "-I" + L.REF_SRC, "-I" + os.path.join(ROOT, "include"), "-o", str(exe),

@@ -29,7 +29,7 @@ def _noalloc(lib):
     return fn
 
 
-@pytest.mark.parametrize("policy", [0, 1])
+@pytest.mark.parametrize("policy", [0, 1, 2])
 def test_noalloc_matches_allocating_entry_point(engine, policy):
     torch = pytest.importorskip("torch")
     lib = load_library()
@@ -65,3 +65,24 @@ def test_noalloc_one_playout_per_board_and_limit(engine):
     too_many = 16384 + 1
     assert fn(d_pos.data_ptr(), None, too_many, 1, 0, 0, d_out.data_ptr(), None) == ERR_INVALID
     assert b"maximum" in lib.gpuai_last_error()
+
+
+def test_noalloc_at_the_maximum_position_count(engine):
+    """Exactly GPUAI_NOALLOC_MAX_POSITIONS positions: the last prefix-sum word
+    of the static array is used."""
+    torch = pytest.importorskip("torch")
+    lib = load_library()
+    fn = _noalloc(lib)
+    npos = 16384
+    pos = engine.random_positions(99, npos, 0, 40)
+    reps = np.random.default_rng(9).integers(0, 4, npos).astype(np.uint32)
+    reps[-1] = 3
+    total = int(reps.sum())
+    d_pos = torch.from_numpy(pos.view(np.int32).copy()).cuda()
+    d_out = torch.empty(total, dtype=torch.int8, device="cuda")
+    torch.cuda.synchronize()
+    for call in range(2):
+        expected = engine.playouts(pos, reps, seed=50 + call, stream_base=5, policy=call)
+        rc = fn(d_pos.data_ptr(), reps.ctypes.data_as(_u32p), npos, 50 + call, 5, call, d_out.data_ptr(), None)
+        assert rc == OK, lib.gpuai_last_error()
+        np.testing.assert_array_equal(d_out.cpu().numpy(), expected)
