@@ -165,6 +165,29 @@ def time_cpu_baseline(positions, min_seconds=10.0, max_seconds=30.0):
                       f"{el:.1f} s, HostPlayoutDriver (src/playout.cpp:17-32)"}
 
 
+def time_cpu_strong(positions, min_seconds=5.0):
+    """The stronger CPU figure: the project's bitboard ply with per-playout
+    Philox streams (oracle/cpu_playouts.cpp) on every host core, on the same
+    positions; its outcomes equal the GPU kernel's."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_lib as L
+    threads = os.cpu_count() or 1
+    reps = np.full(len(positions), 256, dtype=np.uint32)
+    done, plies, t0, k = 0, 0, time.perf_counter(), 0
+    while True:
+        _, pl = L.cpu_playouts(positions, reps, 0xC0DE, k * int(reps.sum()), threads)
+        done += int(reps.sum())
+        plies += pl
+        k += 1
+        el = time.perf_counter() - t0
+        if el >= min_seconds:
+            break
+    return {"value": done / el, "unit": UNIT, "cores": threads, "kind": "project bitboard restatement",
+            "plies_per_s": plies / el,
+            "sample": f"{done} playouts of the same 64 positions, {el:.1f} s, the GPU kernel's bitboard ply and "
+                      "Philox streams on the host (oracle/cpu_playouts.cpp)"}
+
+
 def time_cpu_heuristic(positions, min_seconds=5.0):
     """The reference's HostHeuristicPlayoutDriver (src/heuristicPlayout.cpp:12-48,
     OpenMP over the states) on all of this machine's cores: built from the
@@ -425,6 +448,7 @@ def run_ours(args):
         roof["frac_at_sampled_clock"] = roof["frac"] * sm_mhz / clocks["sm_mhz"]
     if world == 1 and not args.no_cpu:
         line["cpu_baseline"] = time_cpu_baseline(positions)
+        line["cpu_baseline_strong"] = time_cpu_strong(positions)
         pols["ref_heuristic"]["cpu_baseline"] = time_cpu_heuristic(positions)
     print(json.dumps(line), flush=True)
 
@@ -645,7 +669,7 @@ def run_learned(args):
     held-out positions, and a learned-vs-plain MCTS match at equal ms/move."""
     from gpu_ai_gb300 import Engine, Net
     from gpu_ai_gb300 import learn
-    from gpu_ai_gb300.match import play_match
+    from gpu_ai_gb300.match import play_configs, play_match
     peaks, peak_kind = measured_peaks()
     eng = Engine(0)
     t0 = time.perf_counter()
@@ -667,16 +691,31 @@ def run_learned(args):
     step_s = (time.perf_counter() - ts) / k
     tflops = TRAIN_FLOPS_PER_POSITION * 8192 / step_s / 1e12
     ev = learn.evaluate(net, eng, te)
+    if args.save_net:
+        net.save(args.save_net)
+    # the learned player with learned-proposal playouts against plain MCTS, the
+    # same player without the proposal (priors and leaf values only) against
+    # plain MCTS, and the two learned players against each other: the
+    # proposal's own gain
+    mp = play_match(net, eng, n_games=args.match_games, ms_per_move=args.ms, seed=5, leaves=64, plain_ppl=8,
+                    learned_ppl=2, value_weight=0.5, c_puct=1.5, guided=args.guided, temperature=args.temperature)
     m = play_match(net, eng, n_games=args.match_games, ms_per_move=args.ms, seed=5, leaves=64, plain_ppl=8,
                    learned_ppl=2, value_weight=0.5, c_puct=1.5)
+    with_p = {"net": net, "ppl": 2, "value_weight": 0.5, "c_puct": 1.5, "guided": args.guided,
+              "temperature": args.temperature}
+    without_p = {"net": net, "ppl": 2, "value_weight": 0.5, "c_puct": 1.5}
+    head = play_configs(eng, with_p, without_p, n_games=args.match_games, ms_per_move=args.ms, seed=6, leaves=64)
     line = {
         "metric": "learned-proposal MCTS score vs plain GPU MCTS at equal ms/move",
-        "value": m["learned_score"], "unit": "score (win 1, draw 0.5)", "higher_is_better": True, "n_gpus": 1,
+        "value": mp["learned_score"], "unit": "score (win 1, draw 0.5)", "higher_is_better": True, "n_gpus": 1,
         "dtype": "bf16 (fp32 accumulation)", "data": "synthetic (GPU self-play positions, GPU playout labels)",
         "config": {"workload": f"{args.positions} self-play positions x {args.label_playouts} playouts, "
-                               f"{args.epochs} epochs, {args.match_games} games at {args.ms} ms/move",
+                               f"{args.epochs} epochs, {args.match_games} games at {args.ms} ms/move, "
+                               f"{args.guided} guided plies at temperature {args.temperature}",
                    "network": "129-256-256-(1024 logits + tanh value)"},
-        "ci95_wilson": m["ci95_wilson"], "ci95_normal": m["ci95_normal"], "match": m,
+        "ci95_wilson": mp["ci95_wilson"], "ci95_normal": mp["ci95_normal"], "match": mp,
+        "priors_and_value_only_vs_plain": m,
+        "proposal_vs_no_proposal": head,
         "labels": {"positions_kept": int(data["boards"].shape[0]), "seconds": data["label_seconds"],
                    "playouts_per_s": data["playouts"] / data["label_seconds"]},
         "training": {"steps": res["steps"], "batch": res["batch"], "seconds": res["train_seconds"],
@@ -711,6 +750,10 @@ def main():
     ap.add_argument("--epochs", type=float, default=3.0, help="learned workload: training epochs")
     ap.add_argument("--match-games", type=int, default=400, help="learned workload: match games")
     ap.add_argument("--ms", type=float, default=100.0, help="learned workload: milliseconds per move")
+    ap.add_argument("--guided", type=int, default=2,
+                    help="learned workload: plies of every playout drawn from the network's policy")
+    ap.add_argument("--temperature", type=float, default=1.0, help="learned workload: proposal temperature")
+    ap.add_argument("--save-net", default="", help="learned workload: save the trained network to this file")
     ap.add_argument("--rate", type=float, default=1000.0, help="serve workload: requests per second")
     ap.add_argument("--serve-leaves", type=int, default=512,
                     help="serve workload: leaves per search per step (1..512; every request gets the same)")

@@ -8,6 +8,7 @@
 // its longest game (the reference's coarsePlayoutKernel work queue,
 // src/coarsePlayout.cu:73-86, done with one atomicAdd per warp claim instead
 // of a per-thread atomicCAS spin).
+#include "detmath.cuh"
 #include "launch.h"
 #include "rules.cuh"
 
@@ -335,6 +336,110 @@ __global__ void __launch_bounds__(BLOCK) warp_playout_kernel(PlayoutArgs a) {
   if (a.plies != nullptr && lane == 0) atomicAdd(a.plies, plies_here);
 }
 
+// ---- learned-proposal plies (thread per playout)
+
+// One guided ply: the legal moves of playout j's board are weighted by the
+// network's policy -- the softmax at temperature T of each move's (from, to)
+// logit over the legal pairs, a pair's share split equally among the moves
+// that have it -- as integers w = max(1, floor(2^24 e^((l - lmax) / T)) / mult),
+// and the move taken is the first whose running weight sum exceeds
+// mulhi(draw, sum of w).  The draw is draw number `ply` of the playout's
+// stream under tag kTagProposal (the playout's own random moves use tag 0).
+// The float steps are detmath.cuh's, so a CPU replay fed the same logits and
+// draws picks the same move.  A finished game keeps its board.
+__global__ void __launch_bounds__(128) proposal_ply_kernel(ProposalArgs a) {
+  if (a.dev_sizes != nullptr) {
+    a.npos = __ldg(&a.dev_sizes[0]);
+    a.total = __ldg(&a.dev_sizes[1]);
+  }
+  const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j == 0 && a.out_sizes != nullptr) {
+    a.out_sizes[0] = a.total;
+    a.out_sizes[1] = a.total;
+  }
+  if (j >= a.total) return;
+  uint32_t row = j;
+  uint64_t sid = a.stream_base + j;
+  if (a.per_position) {
+    PlayoutArgs pa{};
+    pa.offsets = a.offsets;
+    pa.npos = a.npos;
+    pa.uniform_reps = a.uniform_reps;
+    pa.stream_base = a.stream_base;
+    pa.pos_stream = a.pos_stream;
+    row = position_of(pa, j);
+    sid = stream_of(pa, row, j);
+  } else if (a.play_stream != nullptr) {
+    sid = a.play_stream[j];
+  }
+  Board b = load_board(a.in + row);
+  const uint16_t *lg = a.logits + (size_t)row * 1024u;
+  if (a.trace_boards) a.trace_boards[j] = b;
+  if (a.trace_logits) {
+    const uint4 *src = reinterpret_cast<const uint4 *>(lg);
+    uint4 *dst = reinterpret_cast<uint4 *>(a.trace_logits + (size_t)j * 1024u);
+    for (int q = 0; q < 128; q++) dst[q] = src[q];
+  }
+  if (a.out_stream) a.out_stream[j] = sid;
+  if (((b.meta >> 8) & 0xffu) < (uint32_t)kDrawPlies) {
+    Side sd;
+    make_side(b, sd);
+    const uint32_t J = jumpers(sd);
+    uint32_t c[4] = {a.ply >> 2, (uint32_t)sid, (uint32_t)(sid >> 32), kTagProposal};
+    philox4x32_10(c, (uint32_t)a.seed, (uint32_t)(a.seed >> 32));
+    const uint32_t w = a.ply & 3u;
+    const uint32_t draw = w == 0 ? c[0] : (w == 1 ? c[1] : (w == 2 ? c[2] : c[3]));
+    uint16_t pair[kProposalMaxMoves];
+    int k = 0;
+    float lmax = -3.0e38f;
+    const int n = for_each_move(sd, J, [&](int from, int to, uint32_t, int, uint32_t) {
+      if (k < kProposalMaxMoves) {
+        pair[k] = (uint16_t)(from * 32 + to);
+        lmax = fmaxf(lmax, __uint_as_float((uint32_t)lg[pair[k]] << 16));
+      }
+      k++;
+      return false;
+    });
+    if (n > 0) {
+      uint32_t pick = 0;
+      if (n > kProposalMaxMoves) {
+        pick = mulhi_index(draw, (uint32_t)n);
+      } else if (n >= 2) {
+        uint32_t wt[kProposalMaxMoves];
+        uint32_t sum = 0;
+        for (int m = 0; m < n; m++) {
+          uint32_t mult = 0;
+          for (int q = 0; q < n; q++) mult += pair[q] == pair[m];
+          const float l = __uint_as_float((uint32_t)lg[pair[m]] << 16);
+          const float e = dm::det_exp(dm::mul(dm::sub(l, lmax), a.inv_temperature));
+          const uint32_t v = __float2uint_rz(dm::mul(e, 16777216.0f)) / mult;
+          wt[m] = v > 0u ? v : 1u;
+          sum += wt[m];
+        }
+        const uint32_t r = mulhi_index(draw, sum);
+        uint32_t acc = 0;
+        for (int m = 0; m < n; m++) {
+          acc += wt[m];
+          if (acc > r) {
+            pick = (uint32_t)m;
+            break;
+          }
+        }
+      }
+      uint32_t at = 0;
+      const Board before = b;
+      for_each_move(sd, J, [&](int from, int to, uint32_t removed, int, uint32_t) {
+        if (at++ != pick) return false;
+        b = before;
+        apply_move(b, from, to, removed);
+        return true;
+      });
+    }
+  }
+  uint4 *dst = reinterpret_cast<uint4 *>(a.out + j);
+  *dst = make_uint4(b.p1, b.p2, b.kings, b.meta);
+}
+
 // ---- move lists (thread per board)
 
 __global__ void genmoves_kernel(const Board *pos, uint32_t n, uint8_t *out, uint32_t max_moves,
@@ -422,6 +527,13 @@ cudaError_t launch_playouts(const PlayoutArgs &a, int policy, int block, int gri
   if (layout == kLayoutWarp && policy != 0) return cudaErrorInvalidValue;
   void *args[] = {const_cast<PlayoutArgs *>(&a)};
   return cudaLaunchKernel(playout_fn(policy, block, layout), dim3(grid), dim3(block), args, 0, s);
+}
+
+cudaError_t launch_proposal_ply(const ProposalArgs &a, cudaStream_t s) {
+  const uint32_t grid = (a.total + 127u) / 128u;  // a.total: upper bound when dev_sizes is set
+  if (grid == 0) return cudaSuccess;
+  proposal_ply_kernel<<<grid, 128, 0, s>>>(a);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_genmoves(const Board *pos, uint32_t n, void *out, uint32_t max_moves,

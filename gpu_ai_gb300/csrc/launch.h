@@ -38,6 +38,34 @@ struct PlayoutArgs {
   const uint32_t *dev_sizes = nullptr;
 };
 
+// One guided ply of learned-proposal playouts (kernels.cu, proposal_ply_kernel):
+// every playout's board advances by one move drawn from the network's policy.
+constexpr uint32_t kTagProposal = 2;  // random-stream tag of the guided plies' draws
+constexpr int kProposalMaxMoves = 64; // more legal moves than this: uniform choice
+
+struct ProposalArgs {
+  const Board *in;            // per position (per_position) or per playout
+  const uint32_t *offsets;    // per_position: npos+1 prefix sums, or nullptr for uniform_reps
+  uint32_t npos;
+  uint32_t uniform_reps;
+  uint32_t total;             // playouts
+  const uint32_t *dev_sizes;  // optional {npos, total} read at kernel start
+  bool per_position;          // input boards and logits rows are per position (first guided ply)
+  const uint16_t *logits;     // BF16 bit patterns, 1024 per input row (from * 32 + to)
+  uint64_t seed;
+  uint64_t stream_base;       // stream of playout j: stream_base + j, unless ...
+  const uint64_t *pos_stream; // ... per position first ids (per_position), or
+  const uint64_t *play_stream;// ... per playout ids (later plies)
+  uint32_t ply;               // guided ply index: the draw index on the proposal stream
+  float inv_temperature;
+  Board *out;                 // per playout (may equal `in` when !per_position)
+  uint64_t *out_stream;       // optional: each playout's stream id
+  uint32_t *out_sizes;        // optional: {total, total}
+  Board *trace_boards;        // optional: each playout's board before this ply
+  uint16_t *trace_logits;     // optional: the logits row each playout used
+};
+cudaError_t launch_proposal_ply(const ProposalArgs &a, cudaStream_t s);
+
 // Playout layouts: a thread per playout (every policy) or a warp per playout
 // (uniform random policy only; same outcomes).
 constexpr int kLayoutThread = 0, kLayoutWarp = 1;

@@ -64,6 +64,12 @@ struct gpuai_net {
   uint32_t *status = nullptr;
   gpuai_board *in_boards = nullptr;  // staging for host-buffer calls
   float *in_z = nullptr, *in_q = nullptr;
+  // learned-proposal playouts: a forward workspace with BF16 logits and the
+  // playouts' boards, grown to the largest call so far
+  ga::net::Fwd prop_fw;
+  std::vector<void *> prop_allocs;
+  ga::Board *prop_cur = nullptr;
+  size_t prop_cur_cap = 0;
   std::mutex mu;
 };
 
@@ -996,6 +1002,8 @@ void gpuai_net_destroy(gpuai_net *net) {
   if (!net) return;
   cudaSetDevice(net->device);
   if (net->stream) cudaStreamSynchronize(net->stream);
+  for (void *p : net->prop_allocs) cudaFree(p);
+  if (net->prop_cur) cudaFree(net->prop_cur);
   for (void *p : net->allocs) cudaFree(p);
   if (net->stream) cudaStreamDestroy(net->stream);
   delete net;
@@ -1133,6 +1141,71 @@ int gpuai_net_train_step(gpuai_net *net, const gpuai_board *d_boards, const floa
     return check_status(net);
   }
   return GPUAI_OK;
+}
+
+int gpuai_playouts_learned(gpuai_ctx *ctx, gpuai_net *net, const gpuai_board *d_pos, const uint32_t *d_offsets,
+                           uint32_t npos, uint32_t uniform_reps, uint32_t total, uint64_t seed, uint64_t stream_base,
+                           uint32_t guided_plies, float temperature, int8_t *d_out, void *stream,
+                           gpuai_board *d_trace_boards, uint16_t *d_trace_logits) {
+  if (!ctx || !net) return err(GPUAI_ERR_INVALID, "gpuai_playouts_learned: ctx or net is NULL");
+  if (npos == 0 || total == 0) return GPUAI_OK;
+  if (!d_pos || !d_out) return err(GPUAI_ERR_INVALID, "gpuai_playouts_learned: NULL buffer");
+  if (guided_plies > kMaxGuidedPlies)
+    return err(GPUAI_ERR_INVALID, "gpuai_playouts_learned: guided_plies above " + std::to_string(kMaxGuidedPlies));
+  if (!(temperature > 0.0f && temperature < 1.0e6f))
+    return err(GPUAI_ERR_INVALID, "gpuai_playouts_learned: temperature must be positive");
+  if (!d_offsets && (uint64_t)npos * uniform_reps != total)
+    return err(GPUAI_ERR_INVALID, "gpuai_playouts_learned: total != npos * uniform_reps");
+  if (total > 0x7fffffffu) return err(GPUAI_ERR_INVALID, "gpuai_playouts_learned: more than 2^31-1 playouts");
+  if (guided_plies == 0)
+    return gpuai_playouts_device(ctx, d_pos, d_offsets, npos, uniform_reps, total, seed, stream_base,
+                                 GPUAI_POLICY_RANDOM, d_out, stream);
+  std::lock_guard<std::mutex> lock(net->mu);
+  NCK(cudaSetDevice(net->device), "cudaSetDevice");
+  const cudaStream_t s = static_cast<cudaStream_t>(stream);
+  // workspace: logits for the positions (first guided ply) and for the playouts (later plies)
+  const uint32_t need_rows = round128(guided_plies > 1 && total > npos ? total : npos);
+  if (net->prop_fw.rows < need_rows || net->prop_cur_cap < total) {
+    NCK(cudaDeviceSynchronize(), "workspace");
+    for (void *p : net->prop_allocs) cudaFree(p);
+    net->prop_allocs.clear();
+    net->prop_fw = Fwd();
+    if (net->prop_cur) cudaFree(net->prop_cur);
+    net->prop_cur = nullptr;
+    net->prop_cur_cap = 0;
+    NCK(fwd_alloc(net->prop_fw, need_rows, net->prop_allocs, true), "proposal workspace");
+    NCK(cudaMalloc(&net->prop_cur, (size_t)total * sizeof(ga::Board)), "proposal boards");
+    net->prop_cur_cap = total;
+  }
+  Fwd &W = net->prop_fw;
+  NCK(forward(net, W, d_pos, npos, nullptr, net->status, s), "forward on the positions");
+  ga::ProposalArgs a{};
+  a.in = reinterpret_cast<const ga::Board *>(d_pos);
+  a.offsets = d_offsets;
+  a.npos = npos;
+  a.uniform_reps = uniform_reps;
+  a.total = total;
+  a.per_position = true;
+  a.logits = reinterpret_cast<const uint16_t *>(W.logits_b);
+  a.seed = seed;
+  a.stream_base = stream_base;
+  a.inv_temperature = 1.0f / temperature;
+  a.out = net->prop_cur;
+  for (uint32_t g = 0; g < guided_plies; g++) {
+    if (g > 0) {
+      NCK(forward(net, W, reinterpret_cast<const gpuai_board *>(net->prop_cur), total, nullptr, net->status, s),
+          "forward on the playouts");
+      a.in = net->prop_cur;
+      a.per_position = false;
+      a.offsets = nullptr;
+    }
+    a.ply = g;
+    a.trace_boards = d_trace_boards ? reinterpret_cast<ga::Board *>(d_trace_boards) + (size_t)g * total : nullptr;
+    a.trace_logits = d_trace_logits ? d_trace_logits + (size_t)g * total * kOut : nullptr;
+    NCK(ga::launch_proposal_ply(a, s), "guided ply");
+  }
+  return gpuai_playouts_device(ctx, reinterpret_cast<const gpuai_board *>(net->prop_cur), nullptr, total, 1, total,
+                               seed, stream_base, GPUAI_POLICY_RANDOM, d_out, stream);
 }
 
 int gpuai_label_positions(gpuai_ctx *ctx, const gpuai_board *d_pos, uint32_t n, uint32_t playouts_per_position,

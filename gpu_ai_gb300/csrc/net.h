@@ -33,6 +33,7 @@ constexpr size_t oBV = oWV + kH;
 constexpr size_t kParams = oBV + 1;
 static_assert(kParams == GPUAI_NET_PARAMS, "parameter count");
 
+constexpr uint32_t kMaxGuidedPlies = 32;  // learned-proposal plies per playout at most
 constexpr uint32_t kStatusNetWait = 16u;  // a tensor-core kernel gave up waiting (status bit)
 
 // Forward workspace for up to `rows` boards (a multiple of 128).

@@ -568,6 +568,14 @@ struct gpuai_searches {
   ga::net::Fwd fw;
   cudaStream_t side = nullptr;  // the network's branch of a learned step
   cudaEvent_t fork = nullptr, join = nullptr;
+  // learned-proposal playouts: the first `guided` plies of each playout are
+  // drawn from the network's policy
+  uint32_t guided = 0;
+  float inv_temperature = 1.0f;
+  ga::net::Fwd pfw;               // forward on the playouts' boards (later guided plies)
+  ga::Board *pcur = nullptr;      // each playout's board
+  unsigned long long *pstream = nullptr;  // each playout's stream id
+  uint32_t *psizes = nullptr;     // {playouts, playouts}
 };
 
 namespace {
@@ -623,6 +631,58 @@ int enqueue_step(gpuai_searches *s, uint32_t q) {
   a.pos_stream = reinterpret_cast<const uint64_t *>(s->leaves.stream);
   a.dev_sizes = s->leaves.sizes;
   const uint32_t max_leaves = s->slots * s->qmax;
+  if (s->net && s->guided > 0) {
+    // learned-proposal step: the network's forward on the leaves gives the
+    // priors, the leaf values and the first guided ply of every playout;
+    // later guided plies run the network on the playouts' boards; then the
+    // uniformly random rest of each game
+    SCK(ga::net::forward(s->net, s->fw, reinterpret_cast<const gpuai_board *>(s->leaves.board), 0, s->leaves.sizes,
+                         s->ctl + 1, st),
+        "network forward on the leaves");
+    leaf_eval_kernel<<<(max_leaves + 255) / 256, 256, 0, st>>>(s->pool, s->leaves, s->fw.logits_b, s->fw.vraw,
+                                                               max_leaves);
+    SCK(cudaGetLastError(), "leaf evaluation launch");
+    ProposalArgs pa{};
+    pa.in = reinterpret_cast<const Board *>(s->leaves.board);
+    pa.uniform_reps = s->ppl;
+    pa.total = max_leaves * s->ppl;  // grid bound; the sizes come from device memory
+    pa.dev_sizes = s->leaves.sizes;
+    pa.per_position = true;
+    pa.logits = reinterpret_cast<const uint16_t *>(s->fw.logits_b);
+    pa.seed = s->seed;
+    pa.pos_stream = reinterpret_cast<const uint64_t *>(s->leaves.stream);
+    pa.inv_temperature = s->inv_temperature;
+    pa.out = s->pcur;
+    pa.out_stream = reinterpret_cast<uint64_t *>(s->pstream);
+    pa.out_sizes = s->psizes;
+    for (uint32_t g = 0; g < s->guided; g++) {
+      if (g > 0) {
+        SCK(ga::net::forward(s->net, s->pfw, reinterpret_cast<const gpuai_board *>(s->pcur), 0, s->psizes,
+                             s->ctl + 1, st),
+            "network forward on the playouts");
+        pa.in = s->pcur;
+        pa.per_position = false;
+        pa.dev_sizes = s->psizes;
+        pa.logits = reinterpret_cast<const uint16_t *>(s->pfw.logits_b);
+        pa.pos_stream = nullptr;
+        pa.play_stream = reinterpret_cast<const uint64_t *>(s->pstream);
+        pa.out_stream = nullptr;
+        pa.out_sizes = nullptr;
+      }
+      pa.ply = g;
+      SCK(ga::launch_proposal_ply(pa, st), "guided ply launch");
+    }
+    PlayoutArgs b = a;
+    b.pos = s->pcur;
+    b.uniform_reps = 1;
+    b.pos_stream = reinterpret_cast<const uint64_t *>(s->pstream);
+    b.dev_sizes = s->psizes;
+    SCK(launch_playouts(b, s->policy, kPlayoutBlock, s->sms * s->blocks_per_sm, st), "playout kernel launch");
+    backprop_learned_kernel<<<(max_leaves + 255) / 256, 256, 0, st>>>(s->pool, s->tab, s->leaves, s->ppl,
+                                                                      max_leaves, s->lrn);
+    SCK(cudaGetLastError(), "search kernel launch");
+    return GPUAI_OK;
+  }
   if (s->net) {
     // the network's forward pass and the leaf evaluation do not depend on the
     // playouts: they run on a second stream and fill the SMs that the playout
@@ -865,6 +925,32 @@ int gpuai_searches_set_net(gpuai_searches *s, gpuai_net *net, float value_weight
   s->net = net;
   s->lrn.c_puct = c_puct;
   s->lrn.value_weight = value_weight;
+  if (s->graph) cudaGraphExecDestroy(s->graph);  // the step's launches change
+  s->graph = nullptr;
+  return GPUAI_OK;
+}
+
+int gpuai_searches_set_proposal(gpuai_searches *s, uint32_t guided_plies, float temperature) {
+  if (!s) return err(GPUAI_ERR_INVALID, "gpuai_searches_set_proposal: NULL");
+  if (guided_plies > ga::net::kMaxGuidedPlies)
+    return err(GPUAI_ERR_INVALID, "gpuai_searches_set_proposal: guided_plies above 32");
+  if (!(temperature > 0.0f && temperature < 1.0e6f))
+    return err(GPUAI_ERR_INVALID, "gpuai_searches_set_proposal: temperature must be positive");
+  std::lock_guard<std::mutex> lock(s->mu);
+  if (guided_plies > 0 && !s->net)
+    return err(GPUAI_ERR_INVALID, "gpuai_searches_set_proposal: attach a network first (gpuai_searches_set_net)");
+  for (uint32_t i = 0; i < s->slots; i++)
+    if (s->start[i] >= 0) return err(GPUAI_ERR_INVALID, "gpuai_searches_set_proposal: searches are admitted");
+  SCK(cudaSetDevice(s->device), "cudaSetDevice");
+  const size_t P = (size_t)s->slots * s->qmax * s->ppl;
+  if (guided_plies > 0 && !s->pcur) {
+    SCK(dalloc(s, &s->pcur, P), "proposal boards");
+    SCK(dalloc(s, &s->pstream, P), "proposal streams");
+    SCK(dalloc(s, &s->psizes, 2), "proposal sizes");
+  }
+  if (guided_plies > 1 && !s->pfw.rows) SCK(ga::net::fwd_alloc(s->pfw, (uint32_t)P, s->allocations, true), "network workspace");
+  s->guided = guided_plies;
+  s->inv_temperature = 1.0f / temperature;
   if (s->graph) cudaGraphExecDestroy(s->graph);  // the step's launches change
   s->graph = nullptr;
   return GPUAI_OK;

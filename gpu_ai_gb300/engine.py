@@ -118,6 +118,10 @@ def load_library(path: str = LIB_PATH):
     lib.gpuai_set_layout.argtypes = [vp, ctypes.c_int32, ctypes.c_int32]
     lib.gpuai_get_layout.argtypes = [vp, ctypes.c_int32, _i32p]
     lib.gpuai_searches_set_net.argtypes = [vp, vp, ctypes.c_float, ctypes.c_float]
+    lib.gpuai_playouts_learned.argtypes = [vp, vp, vp, vp, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
+                                           ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint32, ctypes.c_float, vp, vp,
+                                           vp, vp]
+    lib.gpuai_searches_set_proposal.argtypes = [vp, ctypes.c_uint32, ctypes.c_float]
     lib.gpuai_searches_nodes.argtypes = [vp, ctypes.c_int32, ctypes.c_uint32, vp, vp, vp, vp, _u32p]
     lib.gpuai_searches_leaves.argtypes = [vp, ctypes.c_uint32, _u32p, vp, vp, vp, vp, vp, vp, vp]
     for name in header_symbols():
@@ -207,6 +211,16 @@ class Engine:
         """Enqueue playouts on device pointers (no synchronisation)."""
         _check(self.lib.gpuai_playouts_device(self.ctx, d_pos, d_offsets, npos, uniform_reps, total, seed,
                                               stream_base, policy, d_out, stream))
+
+    def playouts_learned(self, net: "Net", d_pos: int, d_offsets: Optional[int], npos: int, uniform_reps: int,
+                         total: int, seed: int, stream_base: int, guided_plies: int, temperature: float, d_out: int,
+                         stream: Optional[int] = None, d_trace_boards: Optional[int] = None,
+                         d_trace_logits: Optional[int] = None):
+        """Enqueue learned-proposal playouts on device pointers (gpuai_playouts_learned):
+        the first `guided_plies` plies drawn from the network's policy, the rest random."""
+        _check(self.lib.gpuai_playouts_learned(self.ctx, net.h, d_pos, d_offsets, npos, uniform_reps, total, seed,
+                                               stream_base, guided_plies, temperature, d_out, stream,
+                                               d_trace_boards, d_trace_logits))
 
     def status(self) -> Tuple[int, int]:
         st = ctypes.c_uint32()
@@ -332,6 +346,11 @@ class Searches:
         """Evaluate leaves with `net` (None: plain playout searches)."""
         _check(self.lib.gpuai_searches_set_net(self.h, net.h if net is not None else None, value_weight, c_puct))
         self.net = net  # keep the network alive while the searches use it
+
+    def set_proposal(self, guided_plies: int, temperature: float = 1.0):
+        """Learned-proposal playouts: the first guided_plies plies of every
+        playout drawn from the attached network's policy (0: off)."""
+        _check(self.lib.gpuai_searches_set_proposal(self.h, guided_plies, temperature))
 
     def nodes(self, slot: int, priors: bool = False):
         """The search's tree, nodes numbered from its root: info (n, 4) = {first

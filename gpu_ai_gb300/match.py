@@ -4,8 +4,11 @@ Both players are device-resident batched searches (gpuai_searches_*) on the
 same GPU: the plain player's leaves are valued by uniformly random playouts and
 its slots split by UCB1 (the reference's GameTree::select rule,
 src/mcts.cpp:63-157); the learned player's leaves are valued by the policy/value
-network (blended with its own playouts) and its slots split by PUCT on the
-network's move priors.
+network (blended with its own playouts), its slots split by PUCT on the
+network's move priors, and with guided plies its playouts are learned-proposal
+playouts (their first plies drawn from the network's policy).  play_configs
+plays any two such players against each other, e.g. the learned player with
+and without the proposal.
 
 All games run at once.  A round has two phases, one per player: the player
 starts a fresh search in every game where it is to move and runs them all
@@ -57,19 +60,39 @@ def openings(eng: Engine, n: int, seed: int, min_plies: int = 2, max_plies: int 
     return np.array(got, np.uint32)
 
 
-def play_match(net: Net, eng: Engine, n_games: int = 400, ms_per_move: float = 100.0, seed: int = 0,
-               leaves: int = 64, plain_ppl: int = 8, learned_ppl: int = 2, value_weight: float = 0.5,
-               c_puct: float = 1.5, node_capacity: int = 131072, max_plies: int = 300, verbose: bool = False) -> dict:
+def _searches(cfg: dict, n_games: int, leaves: int, node_capacity: int, seed: int) -> Searches:
+    """The device searches of one player.  cfg: ppl (playouts per leaf), policy,
+    and for a learned player net, value_weight, c_puct and guided plies /
+    temperature of its learned-proposal playouts."""
+    s = Searches(n_games, n_games * node_capacity, leaves, cfg.get("ppl", 8), cfg.get("policy", POLICY_RANDOM),
+                 seed=seed)
+    if cfg.get("net") is not None:
+        s.set_net(cfg["net"], cfg.get("value_weight", 0.5), cfg.get("c_puct", 1.5))
+        if cfg.get("guided", 0):
+            s.set_proposal(cfg["guided"], cfg.get("temperature", 1.0))
+    return s
+
+
+def describe(cfg: dict) -> dict:
+    d = {k: v for k, v in cfg.items() if k != "net"}
+    d["network"] = cfg.get("net") is not None
+    return d
+
+
+def play_configs(eng: Engine, cfg_a: dict, cfg_b: dict, n_games: int = 400, ms_per_move: float = 100.0,
+                 seed: int = 0, leaves: int = 64, node_capacity: int = 131072, max_plies: int = 300,
+                 verbose: bool = False) -> dict:
+    """Player A against player B, every opening played twice with colours
+    swapped; A's score (win 1, draw 0.5) with 95 % intervals."""
     n_games -= n_games % 2
     opens = openings(eng, n_games // 2, seed)
     boards = np.repeat(opens, 2, axis=0)
-    learned_p1 = np.tile([True, False], n_games // 2)  # learned plays PLAYER_1 in even games
+    a_p1 = np.tile([True, False], n_games // 2)  # A plays PLAYER_1 in even games
     plies = np.zeros(n_games, np.int64)
     result = np.full(n_games, -2, np.int64)  # +1 P1 won, -1 P2 won, 0 draw, -2 running
-    plain = Searches(n_games, n_games * node_capacity, leaves, plain_ppl, POLICY_RANDOM, seed=seed * 2 + 1)
-    learned = Searches(n_games, n_games * node_capacity, leaves, learned_ppl, POLICY_RANDOM, seed=seed * 2 + 2)
-    learned.set_net(net, value_weight, c_puct)
-    stats = {"plain_playouts": 0, "learned_playouts": 0, "plain_steps": 0, "learned_steps": 0, "phases": 0}
+    sides = {"a": _searches(cfg_a, n_games, leaves, node_capacity, seed * 2 + 2),
+             "b": _searches(cfg_b, n_games, leaves, node_capacity, seed * 2 + 1)}
+    stats = {"a_playouts": 0, "b_playouts": 0, "a_steps": 0, "b_steps": 0, "phases": 0}
     t_start = time.perf_counter()
 
     def finish_checks():
@@ -85,13 +108,13 @@ def play_match(net: Net, eng: Engine, n_games: int = 400, ms_per_move: float = 1
 
     finish_checks()
     while np.any(result == -2):
-        for side_learned in (True, False):
+        for key in ("a", "b"):
             live = np.flatnonzero(result == -2)
             p1_to_move = (boards[live, 3] & 1) == 0
-            mine = live[np.where(side_learned, p1_to_move == learned_p1[live], p1_to_move != learned_p1[live])]
+            mine = live[np.where(key == "a", p1_to_move == a_p1[live], p1_to_move != a_p1[live])]
             if len(mine) == 0:
                 continue
-            S = learned if side_learned else plain
+            S = sides[key]
             slots = {}
             for g in mine:
                 slots[g] = S.add(boards[g], 1 << 40, node_capacity, (int(g) << 40) | (int(plies[g]) << 28))
@@ -102,7 +125,6 @@ def play_match(net: Net, eng: Engine, n_games: int = 400, ms_per_move: float = 1
                 S.poll()
                 steps += 2
             done, _ = S.poll()
-            key = "learned" if side_learned else "plain"
             stats[f"{key}_playouts"] += int(sum(int(done[slots[g]]) for g in mine))
             stats[f"{key}_steps"] += steps
             stats["phases"] += 1
@@ -114,22 +136,39 @@ def play_match(net: Net, eng: Engine, n_games: int = 400, ms_per_move: float = 1
             finish_checks()
         if verbose:
             print(f"round: {int(np.sum(result != -2))}/{n_games} finished", flush=True)
-    plain.close()
-    learned.close()
-    lw = int(np.sum((result == 1) & learned_p1) + np.sum((result == -1) & ~learned_p1))
-    ll = int(np.sum((result == -1) & learned_p1) + np.sum((result == 1) & ~learned_p1))
-    ld = int(np.sum(result == 0))
-    score = (lw + 0.5 * ld) / n_games
+    for S in sides.values():
+        S.close()
+    aw = int(np.sum((result == 1) & a_p1) + np.sum((result == -1) & ~a_p1))
+    al = int(np.sum((result == -1) & a_p1) + np.sum((result == 1) & ~a_p1))
+    dr = int(np.sum(result == 0))
+    score = (aw + 0.5 * dr) / n_games
     # per-game score variance for the normal interval (draws count half)
-    per_game = np.where(result == 0, 0.5, np.where((result == 1) == learned_p1, 1.0, 0.0))
+    per_game = np.where(result == 0, 0.5, np.where((result == 1) == a_p1, 1.0, 0.0))
     se = float(per_game.std(ddof=1) / math.sqrt(n_games)) if n_games > 1 else 1.0
-    return {"games": n_games, "ms_per_move": ms_per_move, "learned_wins": lw, "draws": ld, "learned_losses": ll,
-            "learned_score": score, "ci95_normal": [score - 1.96 * se, score + 1.96 * se],
+    return {"games": n_games, "ms_per_move": ms_per_move, "a_wins": aw, "draws": dr, "a_losses": al,
+            "a_score": score, "ci95_normal": [score - 1.96 * se, score + 1.96 * se],
             "ci95_wilson": list(wilson(score, n_games)), "mean_plies": float(plies.mean()),
-            "seconds": time.perf_counter() - t_start,
-            "config": {"leaves_per_search_per_step": leaves, "plain_playouts_per_leaf": plain_ppl,
-                       "learned_playouts_per_leaf": learned_ppl, "value_weight": value_weight, "c_puct": c_puct},
-            **stats}
+            "seconds": time.perf_counter() - t_start, "leaves_per_search_per_step": leaves,
+            "a": describe(cfg_a), "b": describe(cfg_b), **stats}
+
+
+def play_match(net: Net, eng: Engine, n_games: int = 400, ms_per_move: float = 100.0, seed: int = 0,
+               leaves: int = 64, plain_ppl: int = 8, learned_ppl: int = 2, value_weight: float = 0.5,
+               c_puct: float = 1.5, node_capacity: int = 131072, max_plies: int = 300, verbose: bool = False,
+               guided: int = 0, temperature: float = 1.0) -> dict:
+    """The learned player (network priors and leaf values, and with guided > 0
+    learned-proposal playouts) against plain GPU MCTS."""
+    learned = {"net": net, "ppl": learned_ppl, "value_weight": value_weight, "c_puct": c_puct, "guided": guided,
+               "temperature": temperature}
+    plain = {"ppl": plain_ppl}
+    m = play_configs(eng, learned, plain, n_games, ms_per_move, seed, leaves, node_capacity, max_plies, verbose)
+    m.update({"learned_wins": m["a_wins"], "learned_losses": m["a_losses"], "learned_score": m["a_score"],
+              "learned_playouts": m["a_playouts"], "plain_playouts": m["b_playouts"],
+              "learned_steps": m["a_steps"], "plain_steps": m["b_steps"],
+              "config": {"leaves_per_search_per_step": leaves, "plain_playouts_per_leaf": plain_ppl,
+                         "learned_playouts_per_leaf": learned_ppl, "value_weight": value_weight,
+                         "c_puct": c_puct, "guided_plies": guided, "temperature": temperature}})
+    return m
 
 
 def main(argv: Optional[list] = None):
@@ -142,13 +181,16 @@ def main(argv: Optional[list] = None):
     ap.add_argument("--learned-ppl", type=int, default=2)
     ap.add_argument("--value-weight", type=float, default=0.5)
     ap.add_argument("--c-puct", type=float, default=1.5)
+    ap.add_argument("--guided", type=int, default=0, help="learned-proposal plies per playout")
+    ap.add_argument("--temperature", type=float, default=1.0)
     ap.add_argument("--seed", type=int, default=0)
     a = ap.parse_args(argv)
     net = Net(0, max_batch=256)
     net.load(a.net)
     eng = Engine(0)
     print(json.dumps(play_match(net, eng, a.games, a.ms, a.seed, a.leaves, a.plain_ppl, a.learned_ppl,
-                                a.value_weight, a.c_puct, verbose=True)))
+                                a.value_weight, a.c_puct, verbose=True, guided=a.guided,
+                                temperature=a.temperature)))
 
 
 if __name__ == "__main__":

@@ -171,6 +171,15 @@ int gpuai_searches_poll(gpuai_searches *s, uint64_t *done, uint64_t *budget, uin
 int gpuai_searches_children(gpuai_searches *s, int32_t slot, gpuai_move *moves, uint32_t *visits,
                             uint32_t *score2, uint32_t max_children, uint32_t *nchildren, uint32_t *nodes_used);
 
+/* Learned searches whose playouts are learned-proposal playouts
+ * (gpuai_playouts_learned): the first guided_plies plies of every playout are
+ * drawn from the attached network's policy at `temperature` (0 turns it off:
+ * plain playouts of the searches' policy).  The first guided ply uses the
+ * forward pass on the leaves that also gives the priors and leaf values; later
+ * ones run the network on the playouts' boards.  Needs a network attached and
+ * no admitted searches. */
+int gpuai_searches_set_proposal(gpuai_searches *s, uint32_t guided_plies, float temperature);
+
 /* Inspection of the device trees, for tests and tools (no counterpart in the
  * reference, whose GameTree keeps its nodes private).  Synchronise first.
  * gpuai_searches_nodes: the first min(nnodes, max_nodes) nodes of the search in
@@ -256,6 +265,29 @@ int gpuai_net_train_step(gpuai_net *net, const gpuai_board *d_boards, const floa
 int gpuai_label_positions(gpuai_ctx *ctx, const gpuai_board *d_pos, uint32_t n, uint32_t playouts_per_position,
                           uint64_t seed, uint64_t stream_base, int32_t policy, float *d_value, float *d_move_q,
                           uint8_t *d_nmoves, void *stream);
+/* Learned-proposal playouts (no counterpart in the reference; the shape of its
+ * heuristicPlayoutKernel, src/heuristicPlayout.cu:54-88, with the network's
+ * policy in place of scoreMove): the first guided_plies plies of every playout
+ * are drawn from the network's policy -- the softmax at `temperature` of each
+ * legal move's (from, to) logit over the legal pairs, a pair's share split
+ * equally among the moves that have it, as integer weights
+ * max(1, floor(2^24 e^((l - lmax) / T)) / multiplicity) -- and the rest of the
+ * game is uniformly random (GPUAI_POLICY_RANDOM), the fallback and judge of the
+ * network.  Guided ply g of playout j takes draw g of random stream
+ * (seed, stream_base + j, tag 2); its random plies use stream
+ * (seed, stream_base + j, tag 0) from the board after the guided plies, as
+ * gpuai_playouts does.  Device buffers as gpuai_playouts_device, enqueued on
+ * `stream` without synchronising; guided_plies == 0 is plain random playouts,
+ * at most 32.  The network keeps a workspace sized for the largest call so far
+ * (growing it synchronises the device).  d_trace_boards / d_trace_logits
+ * (optional, device, guided_plies * total entries: boards, and 1024 BF16 bit
+ * patterns each) receive each playout's board before every guided ply and the
+ * logits it was drawn from, for tests that replay the choices. */
+int gpuai_playouts_learned(gpuai_ctx *ctx, gpuai_net *net, const gpuai_board *d_pos, const uint32_t *d_offsets,
+                           uint32_t npos, uint32_t uniform_reps, uint32_t total, uint64_t seed, uint64_t stream_base,
+                           uint32_t guided_plies, float temperature, int8_t *d_out, void *stream,
+                           gpuai_board *d_trace_boards, uint16_t *d_trace_logits);
+
 /* Learned searches: leaves are also evaluated by `net` (NULL turns it off).
  * Each leaf's value is value_weight * net value + (1 - value_weight) * its
  * playout mean; a node's moves get the net's softmax over its legal moves as

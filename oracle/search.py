@@ -353,11 +353,13 @@ class SearchesOracle:
             frontier = nxt
         return leaves
 
-    def step(self, Q: int, net_value=None, net_logits=None):
+    def step(self, Q: int, net_value=None, net_logits=None, outcomes=None):
         """One step over all searches.  Returns the leaf slots [(slot, node,
         board, first stream id, outcomes)] in the device's slot order.  For
         learned searches net_value / net_logits hold the network's raw value
-        and float32 logits per leaf slot, in that order."""
+        and float32 logits per leaf slot, in that order.  `outcomes` (slots x
+        playouts per leaf), when given, stands in for the replayed playouts
+        (learned-proposal playouts, whose parity is checked on their own)."""
         qs = self.quota(Q)
         slots = []
         for si, (s, q) in enumerate(zip(self.slots, qs)):
@@ -368,7 +370,12 @@ class SearchesOracle:
             for i, n in enumerate(leaves):
                 slots.append([si, n, s.nodes[n].board, s.stream_next + i * self.ppl, None])
             s.stream_next += q * self.ppl
-        self._playouts(slots)
+        if outcomes is None:
+            self._playouts(slots)
+        else:
+            assert len(outcomes) == len(slots)
+            for sl, o in zip(slots, outcomes):
+                sl[4] = np.asarray(o, np.int8)
         if self.learned is not None:
             values = self._leaf_eval(slots, net_value, net_logits)
             self._backprop_learned(slots, values)

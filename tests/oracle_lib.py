@@ -18,6 +18,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 ORACLE_DIR = os.path.join(ROOT, "oracle")
 ORACLE_SO = os.path.join(ORACLE_DIR, "_build", "liboracle.so")
 REF_SO = os.path.join(ORACLE_DIR, "_ref", "libref.so")
+CPU_SO = os.path.join(ORACLE_DIR, "_build", "libcpu_playouts.so")
 # the reference's sources, where present (GPUAI_REFERENCE_SRC overrides)
 REF_SRC = os.environ.get("GPUAI_REFERENCE_SRC", "/root/reference/src")
 
@@ -198,6 +199,31 @@ def replay_one(pos_row, seed, sid, policy=0):
     o = oracle().or_replay_playout(_ptr(p, _u32p), seed, sid, policy, _ptr(plies, _u32p),
                                    _ptr(draws, _u32p))
     return o, int(plies[0]), int(draws[0])
+
+
+_cpu = None
+
+
+def cpu_playouts(pos, reps, seed, stream_base=0, nthreads=0):
+    """The stronger CPU baseline (oracle/cpu_playouts.cpp): the project's
+    bitboard ply with the GPU's random streams on every host core.  Returns
+    (outcomes, plies)."""
+    global _cpu
+    if _cpu is None:
+        src = os.path.join(ORACLE_DIR, "cpu_playouts.cpp")
+        if not os.path.exists(CPU_SO) or os.path.getmtime(CPU_SO) < os.path.getmtime(src):
+            build_oracle()
+        lib = ctypes.CDLL(CPU_SO)
+        lib.cp_playouts.argtypes = [_u32p, _u32p, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_uint64, _i8p,
+                                    ctypes.c_int]
+        lib.cp_playouts.restype = ctypes.c_uint64
+        _cpu = lib
+    pos = np.ascontiguousarray(pos, dtype=np.uint32).reshape(-1, 4)
+    reps = np.ascontiguousarray(reps, dtype=np.uint32)
+    out = np.zeros(int(reps.sum()), dtype=np.int8)
+    plies = _cpu.cp_playouts(_ptr(pos, _u32p), _ptr(reps, _u32p), pos.shape[0], seed, stream_base,
+                             _ptr(out, _i8p), nthreads)
+    return out, int(plies)
 
 
 def host_playouts_port(states, nthreads=0, srand_seed=1):

@@ -114,10 +114,12 @@ def _peaky_params(seed):
     return mlp.pack(d).astype(np.float32)
 
 
-@pytest.mark.parametrize("ppl,graph", [(2, True), (1, False)])
-def test_learned_searches_node_for_node(ppl, graph):
+@pytest.mark.parametrize("ppl,graph,guided", [(2, True, 0), (1, False, 0), (2, True, 3)])
+def test_learned_searches_node_for_node(ppl, graph, guided):
     """PUCT split with the network's priors, expansion once evaluated, and the
-    blended leaf value, with a fixed network."""
+    blended leaf value, with a fixed network; with guided plies the playouts
+    are learned-proposal playouts (their outcomes are taken from the GPU: the
+    proposal playouts are replayed on their own in test_gpu_proposal.py)."""
     from gpu_ai_gb300 import Net, Searches
     q = 32
     params = _peaky_params(5)
@@ -126,6 +128,8 @@ def test_learned_searches_node_for_node(ppl, graph):
     roots = list(L.random_positions(25, 3, 0, 30))
     gpu = Searches(4, 200000, q, playouts_per_leaf=ppl, policy=0, seed=3)
     gpu.set_net(net, value_weight=0.5, c_puct=1.5)
+    if guided:
+        gpu.set_proposal(guided, 1.0)
     learned = {"value_weight": 0.5, "c_puct": 1.5}
     o = S.SearchesOracle(4, ppl, 0, 3, children=L.children, playouts=_replay, learned=learned)
     budgets = [300, 500, 200]
@@ -144,7 +148,8 @@ def test_learned_searches_node_for_node(ppl, graph):
             scale = float(np.abs(ref["logits"]).max())
             assert np.abs(lv["net_logits"] - ref["logits"]).max() <= 2e-2 * scale
             assert np.abs(lv["net_value"] - ref["vraw"]).max() <= 2e-2 * max(1.0, float(np.abs(ref["vraw"]).max()))
-        o.step(q, net_value=lv["net_value"], net_logits=lv["net_logits"])
+        o.step(q, net_value=lv["net_value"], net_logits=lv["net_logits"],
+               outcomes=lv["outcomes"] if guided else None)
         _compare_step(gpu, o, step, net=True)
         _compare_trees(gpu, o, slots, step, priors=True)
         if all(o.slots[k].done >= o.slots[k].budget for k in slots):

@@ -129,3 +129,14 @@ def test_apply_matches_reference_live():
         b = pos[i].copy()
         assert lib.ref_apply_b16(b.ctypes.data_as(L._u32p), k) == 0
         np.testing.assert_array_equal(a, b)
+
+
+def test_stronger_cpu_baseline_equals_the_replay():
+    """The stronger CPU baseline (the kernel's bitboard ply on the host with the
+    GPU's streams) gives every playout the outcome of the oracle's replay."""
+    pos = L.random_positions(2016, 64, 0, 30)
+    reps = np.full(64, 24, dtype=np.uint32)
+    out, plies = L.cpu_playouts(pos, reps, 0x5EED, 77)
+    exp, pl = L.replay_batch(pos, reps, 0x5EED, 77, 0)
+    np.testing.assert_array_equal(out, exp)
+    assert plies == int(pl.sum())
