@@ -4,6 +4,11 @@ Everything is compiled in-tree with nvcc/g++ directly (no cmake):
 
   gpu_ai_gb300/lib/libgpuai.so   kernels + C ABI (include/gpuai.h)
   gpu_ai_gb300/lib/run_ai        the run_ai driver (playout/game tests, players)
+  gpu_ai_gb300/lib/libgpuai_checked.so  (build(checks=True)) the same library with
+                                 the kernels' bounds checks compiled in
+                                 (-DGPUAI_CHECKS): a failed check skips the
+                                 access and sets a status bit, reported as
+                                 GPUAI_ERR_LIMIT; load it with GPUAI_LIB=<path>
 
 Translation units are compiled in parallel; a unit is rebuilt only when one of
 its inputs is newer than its object.
@@ -65,36 +70,42 @@ def _host_units():
     return sorted(f for f in os.listdir(HOST) if f.endswith(".cpp") and f != "run_ai.cpp")
 
 
-def build(verbose: bool = False) -> str:
-    """Compile libgpuai.so (and run_ai when the host sources exist); return the .so path."""
+def build(verbose: bool = False, checks: bool = False) -> str:
+    """Compile libgpuai.so (and run_ai when the host sources exist); return the
+    .so path.  checks=True builds libgpuai_checked.so instead: the same code
+    with the kernels' bounds checks (-DGPUAI_CHECKS)."""
     os.makedirs(LIB, exist_ok=True)
-    os.makedirs(OBJ, exist_ok=True)
+    obj_dir = OBJ + ("_checked" if checks else "")
+    os.makedirs(obj_dir, exist_ok=True)
+    extra = ["-DGPUAI_CHECKS"] if checks else []
     hdrs = _headers(CSRC) + _headers(INCLUDE) + (_headers(HOST) if os.path.isdir(HOST) else [])
     jobs = []
     objs = []
     for u in CUDA_UNITS:
         src = os.path.join(CSRC, u)
-        obj = os.path.join(OBJ, u + ".o")
+        obj = os.path.join(obj_dir, u + ".o")
         objs.append(obj)
         if _stale(obj, [src] + hdrs + [__file__]):
-            jobs.append([nvcc()] + NVCC_FLAGS + ["-c", src, "-o", obj])
+            jobs.append([nvcc()] + NVCC_FLAGS + extra + ["-c", src, "-o", obj])
     host_objs = []
     for u in _host_units():
         src = os.path.join(HOST, u)
-        obj = os.path.join(OBJ, u + ".o")
+        obj = os.path.join(obj_dir, u + ".o")
         host_objs.append(obj)
         if _stale(obj, [src] + hdrs + [__file__]):
-            jobs.append(["g++"] + CXX_FLAGS + ["-c", src, "-o", obj])
+            jobs.append(["g++"] + CXX_FLAGS + extra + ["-c", src, "-o", obj])
     run_ai_src = os.path.join(HOST, "run_ai.cpp")
     run_ai_obj = os.path.join(OBJ, "run_ai.cpp.o")
-    if os.path.exists(run_ai_src) and _stale(run_ai_obj, [run_ai_src] + hdrs + [__file__]):
+    if not checks and os.path.exists(run_ai_src) and _stale(run_ai_obj, [run_ai_src] + hdrs + [__file__]):
         jobs.append(["g++"] + CXX_FLAGS + ["-c", run_ai_src, "-o", run_ai_obj])
     with ThreadPoolExecutor(max_workers=max(1, min(8, len(jobs)))) as ex:
         list(ex.map(lambda c: _run(c, verbose), jobs))
-    so = os.path.join(LIB, "libgpuai.so")
+    so = os.path.join(LIB, "libgpuai_checked.so" if checks else "libgpuai.so")
     all_objs = objs + host_objs
     if _stale(so, all_objs):
         _run([nvcc(), "-shared", "-Xcompiler", "-fPIC"] + ARCH + ["-o", so] + all_objs + ["-lpthread"], verbose)
+    if checks:
+        return so
     if os.path.exists(run_ai_src):
         exe = os.path.join(LIB, "run_ai")
         if _stale(exe, [run_ai_obj, so]):
@@ -103,4 +114,4 @@ def build(verbose: bool = False) -> str:
 
 
 if __name__ == "__main__":
-    print(build(verbose="-v" in sys.argv))
+    print(build(verbose="-v" in sys.argv, checks="--checks" in sys.argv))

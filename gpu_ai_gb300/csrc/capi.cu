@@ -290,6 +290,7 @@ int gpuai_get_launch(gpuai_ctx *ctx, int32_t policy, int32_t *block_threads, int
 
 int gpuai_playouts(gpuai_ctx *ctx, const gpuai_board *pos, const uint32_t *reps, uint32_t npos,
                    uint64_t seed, uint64_t stream_base, int32_t policy, int8_t *out) {
+  GPUAI_RANGE("gpuai_playouts");
   if (!ctx) return fail(GPUAI_ERR_INVALID, "gpuai_playouts: ctx is NULL");
   if (npos == 0) return GPUAI_OK;
   if (!pos || !out) return fail(GPUAI_ERR_INVALID, "gpuai_playouts: NULL buffer");
@@ -359,6 +360,7 @@ int gpuai_playouts(gpuai_ctx *ctx, const gpuai_board *pos, const uint32_t *reps,
 int gpuai_playouts_device(gpuai_ctx *ctx, const gpuai_board *d_pos, const uint32_t *d_offsets,
                           uint32_t npos, uint32_t uniform_reps, uint32_t total, uint64_t seed,
                           uint64_t stream_base, int32_t policy, int8_t *d_out, void *stream) {
+  GPUAI_RANGE("gpuai_playouts_device");
   if (!ctx) return fail(GPUAI_ERR_INVALID, "gpuai_playouts_device: ctx is NULL");
   if (total == 0) return GPUAI_OK;
   if (npos == 0 || !d_pos || !d_out) return fail(GPUAI_ERR_INVALID, "gpuai_playouts_device: empty or NULL input");
@@ -391,6 +393,7 @@ int gpuai_status(gpuai_ctx *ctx, uint32_t *status, uint64_t *plies) {
 
 int gpuai_genmoves(gpuai_ctx *ctx, const gpuai_board *pos, uint32_t n, gpuai_move *out,
                    uint32_t max_moves, uint8_t *counts) {
+  GPUAI_RANGE("gpuai_genmoves");
   if (!ctx) return fail(GPUAI_ERR_INVALID, "gpuai_genmoves: ctx is NULL");
   if (n == 0) return GPUAI_OK;
   if (!pos || !out || !counts || max_moves == 0) return fail(GPUAI_ERR_INVALID, "gpuai_genmoves: NULL buffer");
@@ -422,6 +425,7 @@ int gpuai_genmoves(gpuai_ctx *ctx, const gpuai_board *pos, uint32_t n, gpuai_mov
 
 int gpuai_random_positions(gpuai_ctx *ctx, uint64_t seed, uint32_t n, uint32_t min_plies,
                            uint32_t max_plies, gpuai_board *out) {
+  GPUAI_RANGE("gpuai_random_positions");
   if (!ctx) return fail(GPUAI_ERR_INVALID, "gpuai_random_positions: ctx is NULL");
   if (n == 0) return GPUAI_OK;
   if (!out) return fail(GPUAI_ERR_INVALID, "gpuai_random_positions: out is NULL");
@@ -442,6 +446,7 @@ int gpuai_random_positions(gpuai_ctx *ctx, uint64_t seed, uint32_t n, uint32_t m
 
 int gpuai_selfplay_positions(gpuai_ctx *ctx, uint64_t seed, uint32_t n, uint32_t min_plies, uint32_t max_plies,
                              int32_t policy, gpuai_board *d_out, void *stream) {
+  GPUAI_RANGE("gpuai_selfplay_positions");
   if (!ctx) return fail(GPUAI_ERR_INVALID, "gpuai_selfplay_positions: ctx is NULL");
   if (n == 0) return GPUAI_OK;
   if (!d_out) return fail(GPUAI_ERR_INVALID, "gpuai_selfplay_positions: d_out is NULL");

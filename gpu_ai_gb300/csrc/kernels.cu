@@ -120,7 +120,7 @@ __global__ void __launch_bounds__(BLOCK, (playout_min_blocks<POLICY, BLOCK>())) 
         if (claim(a, have, j, exhausted, lane)) {
           have = true;
           const uint32_t p = position_of(a, j);
-          b = load_board(a.pos + p);
+          if (GA_IN_BOUNDS(p < a.npos, a.status)) b = load_board(a.pos + p);
           rs.start(a.seed, stream_of(a, p, j), 0);
           game_plies = 0;
         }
@@ -132,7 +132,7 @@ __global__ void __launch_bounds__(BLOCK, (playout_min_blocks<POLICY, BLOCK>())) 
         if (!have) break;
         if ((pend == 1u && !men_ok) || (pend == 2u && !king_ok)) break;  // still deferred
         if (((b.meta >> 8) & 0xffu) >= (uint32_t)kDrawPlies) {
-          a.out[j] = 0;
+          if (GA_IN_BOUNDS(j < a.total, a.status)) a.out[j] = 0;
           have = false;
           break;
         }
@@ -158,7 +158,8 @@ __global__ void __launch_bounds__(BLOCK, (playout_min_blocks<POLICY, BLOCK>())) 
         }
         if (n < 0) atomicOr(a.status, kStatusDepth);
         else if (n > 0) atomicOr(a.status, kStatusPlyCap);
-        a.out[j] = (int8_t)(n == 0 ? ((b.meta & 1u) ? 1 : -1) : 0);  // side to move cannot move: loses
+        if (GA_IN_BOUNDS(j < a.total, a.status))
+          a.out[j] = (int8_t)(n == 0 ? ((b.meta & 1u) ? 1 : -1) : 0);  // side to move cannot move: loses
         have = false;
       } while (false);
 

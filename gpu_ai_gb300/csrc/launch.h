@@ -2,6 +2,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 #include <stdint.h>
 
 #include "rules.cuh"
@@ -12,6 +13,22 @@ namespace ga {
 constexpr uint32_t kStatusDepth = 1u;     // capture sequence deeper than kMaxDepth
 constexpr uint32_t kStatusOverflow = 2u;  // move list longer than the caller's buffer
 constexpr uint32_t kStatusPlyCap = 4u;    // playout exceeded kMaxPlies (cannot happen under the 50-ply rule)
+constexpr uint32_t kStatusBounds = 32u;   // a bounds check of a GPUAI_CHECKS build failed (the access was skipped)
+
+// Bounds checks of the checked build (compiled with -DGPUAI_CHECKS,
+// libgpuai_checked.so): GA_IN_BOUNDS(cond, status) is `cond`, and a failed
+// check sets kStatusBounds in *status; the caller skips the access.  Warp-
+// collective code keeps running on every lane.  In the normal build the
+// checks compile to `true`.
+#if defined(GPUAI_CHECKS) && defined(__CUDA_ARCH__)
+__device__ __forceinline__ bool ga_in_bounds(bool ok, uint32_t *status) {
+  if (!ok && status != nullptr) atomicOr(status, kStatusBounds);
+  return ok;
+}
+#define GA_IN_BOUNDS(cond, status) (::ga::ga_in_bounds((cond), (status)))
+#else
+#define GA_IN_BOUNDS(cond, status) (true)
+#endif
 
 constexpr int kPlayoutBlock = 256;        // default threads per block
 constexpr uint32_t kMaxPlies = 4096;
@@ -84,5 +101,15 @@ cudaError_t launch_random_positions(uint64_t seed, uint32_t n, uint32_t min_plie
 
 // Sets the calling thread's gpuai_last_error() message; returns code.
 int record_error(int code, const char *msg);
+
+// An NVTX range over one C-ABI call (visible in Nsight Systems timelines;
+// without a tool attached a push/pop costs a few nanoseconds).
+struct ApiRange {
+  explicit ApiRange(const char *name) { nvtxRangePushA(name); }
+  ~ApiRange() { nvtxRangePop(); }
+  ApiRange(const ApiRange &) = delete;
+  ApiRange &operator=(const ApiRange &) = delete;
+};
+#define GPUAI_RANGE(name) ::ga::ApiRange gpuai_api_range_(name)
 
 }  // namespace ga

@@ -115,6 +115,8 @@ struct GemmArgs {
   const uint32_t *dev_rows;  // optional device row count: tiles past it do nothing
   uint32_t *status;
   Epi e;
+  uint64_t wait_ns;     // limit of every barrier wait (tc::kWaitLimitNs)
+  uint32_t skip_loads;  // self-test of the bounded waits: issue no TMA load, so the MMA warp's wait runs out
 };
 
 constexpr uint32_t kBM = 128, kBK = 64, kMaxStages = 4;
@@ -254,10 +256,10 @@ __global__ void __launch_bounds__(kThreads, 2)
   uint32_t issued = 0;
 
   if (warp == 0) {
-    if (lane == 0) {  // TMA producer
+    if (lane == 0 && !g.skip_loads) {  // TMA producer
       for (uint32_t i = 0; i < nkb; i++) {
         const uint32_t s = i % nst;
-        if (i >= nst && !tc::mbar_wait(&empty[s], ((i / nst) - 1u) & 1u)) {
+        if (i >= nst && !tc::mbar_wait(&empty[s], ((i / nst) - 1u) & 1u, g.wait_ns)) {
           atomicOr(s_err, 1u);
           break;
         }
@@ -274,7 +276,7 @@ __global__ void __launch_bounds__(kThreads, 2)
       const uint32_t idesc = tc::idesc_bf16_f32(kBM, bn);
       for (uint32_t i = 0; i < nkb; i++) {
         const uint32_t s = i % nst;
-        if (!tc::mbar_wait(&full[s], (i / nst) & 1u)) {
+        if (!tc::mbar_wait(&full[s], (i / nst) & 1u, g.wait_ns)) {
           atomicOr(s_err, 1u);
           break;
         }
@@ -293,7 +295,7 @@ __global__ void __launch_bounds__(kThreads, 2)
 
   // epilogue: warp w reads TMEM lane quadrant w % 4 (tile rows 32(w%4)..) and
   // column half w / 4 of the tile
-  if (!tc::mbar_wait(accf, 0)) atomicOr(s_err, 1u);
+  if (!tc::mbar_wait(accf, 0, g.wait_ns)) atomicOr(s_err, 1u);
   __syncwarp();  // lanes leave the wait one by one; tcgen05.ld needs the whole warp
   tc::fence_after_sync();
   const uint32_t quad = warp & 3u, half = warp >> 2;
@@ -653,7 +655,7 @@ cudaError_t make_map(CUtensorMap *m, const void *base, uint64_t rows, uint64_t k
 
 cudaError_t gemm(const CUtensorMap &a, const CUtensorMap &b, uint32_t m_rows, uint32_t n_total, uint32_t bn,
                  uint32_t kb_total, uint32_t splits, const uint32_t *dev_rows, uint32_t *status, const Epi &e,
-                 cudaStream_t s) {
+                 cudaStream_t s, uint64_t wait_ns = tc::kWaitLimitNs, bool skip_loads = false) {
   if (m_rows % kBM || bn % 64 || bn == 0 || bn > 256 || n_total % bn || splits == 0 || kb_total % splits)
     return cudaErrorInvalidValue;
   if ((e.flags & kEpiVdot) && n_total != bn) return cudaErrorInvalidValue;  // the value head needs whole rows
@@ -669,6 +671,8 @@ cudaError_t gemm(const CUtensorMap &a, const CUtensorMap &b, uint32_t m_rows, ui
   g.dev_rows = dev_rows;
   g.status = status;
   g.e = e;
+  g.wait_ns = wait_ns;
+  g.skip_loads = skip_loads ? 1u : 0u;
   const uint32_t smem = g.stages * stage_bytes + kSmemExtra;
   if (smem > kSmemLimit) return cudaErrorInvalidValue;
   gemm_kernel<<<dim3(m_rows / kBM, n_total / bn, splits), kThreads, smem, s>>>(a, b, g);
@@ -1083,6 +1087,7 @@ int gpuai_net_load(gpuai_net *net, const char *path) {
 }
 
 int gpuai_net_forward(gpuai_net *net, const gpuai_board *boards, uint32_t n, float *value, float *logits) {
+  GPUAI_RANGE("gpuai_net_forward");
   if (!net || (n && (!boards || !value))) return err(GPUAI_ERR_INVALID, "gpuai_net_forward: NULL");
   std::lock_guard<std::mutex> lock(net->mu);
   NCK(cudaSetDevice(net->device), "cudaSetDevice");
@@ -1107,6 +1112,7 @@ int gpuai_net_forward(gpuai_net *net, const gpuai_board *boards, uint32_t n, flo
 
 int gpuai_net_gradients(gpuai_net *net, const gpuai_board *boards, const float *value_target, const float *move_q,
                         uint32_t n, float tau, float value_coef, float *grads, float *loss2) {
+  GPUAI_RANGE("gpuai_net_gradients");
   if (!net || !boards || !value_target || !move_q || !grads) return err(GPUAI_ERR_INVALID, "gpuai_net_gradients: NULL");
   if (n == 0 || n > net->rows) return err(GPUAI_ERR_INVALID, "gpuai_net_gradients: n outside 1..max_batch");
   if (!(tau > 0.0f)) return err(GPUAI_ERR_INVALID, "gpuai_net_gradients: tau must be > 0");
@@ -1126,6 +1132,7 @@ int gpuai_net_gradients(gpuai_net *net, const gpuai_board *boards, const float *
 
 int gpuai_net_train_step(gpuai_net *net, const gpuai_board *d_boards, const float *d_value_target,
                          const float *d_move_q, uint32_t n, float lr, float tau, float value_coef, float *loss2) {
+  GPUAI_RANGE("gpuai_net_train_step");
   if (!net || !d_boards || !d_value_target || !d_move_q) return err(GPUAI_ERR_INVALID, "gpuai_net_train_step: NULL");
   if (n == 0 || n > net->rows) return err(GPUAI_ERR_INVALID, "gpuai_net_train_step: n outside 1..max_batch");
   if (!(tau > 0.0f) || !(lr >= 0.0f)) return err(GPUAI_ERR_INVALID, "gpuai_net_train_step: bad tau or lr");
@@ -1143,10 +1150,37 @@ int gpuai_net_train_step(gpuai_net *net, const gpuai_board *d_boards, const floa
   return GPUAI_OK;
 }
 
+int gpuai_net_wait_selftest(gpuai_net *net, uint32_t wait_limit_us, uint32_t *status) {
+  if (!net || !status) return err(GPUAI_ERR_INVALID, "gpuai_net_wait_selftest: NULL");
+  if (wait_limit_us == 0 || wait_limit_us > 1000000u)
+    return err(GPUAI_ERR_INVALID, "gpuai_net_wait_selftest: wait_limit_us must be in 1..1000000");
+  std::lock_guard<std::mutex> lock(net->mu);
+  NCK(cudaSetDevice(net->device), "cudaSetDevice");
+  const cudaStream_t s = net->stream;
+  // the first layer's GEMM on one 128-row tile, with no TMA load issued: the
+  // MMA warp's wait for the first stage runs out after wait_limit_us
+  Epi e1;
+  e1.flags = kEpiBias | kEpiRelu | kEpiB16;
+  e1.bias = net->params + oB1;
+  e1.out_b = net->fw.H1;
+  e1.ld_b = kH;
+  NCK(gemm(net->fw.mX, net->mW1, kBM, kH, kBnF1, kInPad / kBK, 1, nullptr, net->status, e1, s,
+           (uint64_t)wait_limit_us * 1000u, true),
+      "self-test launch");
+  uint32_t st = 0;
+  NCK(cudaMemcpyAsync(&st, net->status, sizeof st, cudaMemcpyDeviceToHost, s), "status read");
+  NCK(cudaStreamSynchronize(s), "self-test kernel");
+  NCK(cudaMemsetAsync(net->status, 0, sizeof(uint32_t), s), "status clear");
+  NCK(cudaStreamSynchronize(s), "status clear");
+  *status = st;
+  return GPUAI_OK;
+}
+
 int gpuai_playouts_learned(gpuai_ctx *ctx, gpuai_net *net, const gpuai_board *d_pos, const uint32_t *d_offsets,
                            uint32_t npos, uint32_t uniform_reps, uint32_t total, uint64_t seed, uint64_t stream_base,
                            uint32_t guided_plies, float temperature, int8_t *d_out, void *stream,
                            gpuai_board *d_trace_boards, uint16_t *d_trace_logits) {
+  GPUAI_RANGE("gpuai_playouts_learned");
   if (!ctx || !net) return err(GPUAI_ERR_INVALID, "gpuai_playouts_learned: ctx or net is NULL");
   if (npos == 0 || total == 0) return GPUAI_OK;
   if (!d_pos || !d_out) return err(GPUAI_ERR_INVALID, "gpuai_playouts_learned: NULL buffer");
@@ -1211,6 +1245,7 @@ int gpuai_playouts_learned(gpuai_ctx *ctx, gpuai_net *net, const gpuai_board *d_
 int gpuai_label_positions(gpuai_ctx *ctx, const gpuai_board *d_pos, uint32_t n, uint32_t playouts_per_position,
                           uint64_t seed, uint64_t stream_base, int32_t policy, float *d_value, float *d_move_q,
                           uint8_t *d_nmoves, void *stream) {
+  GPUAI_RANGE("gpuai_label_positions");
   if (!ctx) return err(GPUAI_ERR_INVALID, "gpuai_label_positions: ctx is NULL");
   if (n == 0) return GPUAI_OK;
   if (!d_pos || !d_value || !d_move_q || !d_nmoves) return err(GPUAI_ERR_INVALID, "gpuai_label_positions: NULL");

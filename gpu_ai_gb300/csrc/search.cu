@@ -71,6 +71,7 @@ constexpr float kFpuReduction = 0.1f;  // unvisited child's Q = parent's Q - thi
 constexpr float kTerminalLeaf = 2.0f;  // leaf value marking a finished game
 
 struct Pool {  // one entry per node
+  uint32_t nodes;  // capacity (bounds checks of the checked build)
   uint4 *info;   // {first child, nchild | state << 16, visits, score2}
   uint4 *board;
   int32_t *parent;
@@ -96,6 +97,7 @@ struct Leaves {
 struct Learned {
   float c_puct;
   float value_weight;
+  uint32_t max_leaves;  // leaf slots per search and step at most (bounds checks of the checked build)
 };
 
 __device__ __forceinline__ bool board_terminal(const Board &b) {
@@ -352,7 +354,7 @@ __global__ void __launch_bounds__(32 * kSelectWarps) select_kernel(Pool p, Table
       }
       const bool fits = grow > 0 && node_next + (int32_t)gx <= node_end;
       const uint32_t fit_end = __reduce_max_sync(0xffffffffu, fits ? gx : 0u);
-      if (fits) {
+      if (fits && GA_IN_BOUNDS(node_next + (int32_t)gx <= node_end && (uint32_t)node_end <= p.nodes, status)) {
         first = node_next + (int32_t)gx - grow;
         k = grow;
         expand_at(p, n, first, k);
@@ -386,6 +388,7 @@ __global__ void __launch_bounds__(32 * kSelectWarps) select_kernel(Pool p, Table
           const uint4 bv = p.board[n];
           for (uint32_t r = 0; r < leaf; r++) {
             const uint32_t o = off + leaf_at + r;
+            if (!GA_IN_BOUNDS(o < slots * lrn.max_leaves && leaf_at + r < q, status)) break;
             l.board[o] = bv;
             l.node[o] = n;
             l.search[o] = (int32_t)s;
@@ -394,6 +397,7 @@ __global__ void __launch_bounds__(32 * kSelectWarps) select_kernel(Pool p, Table
           uint32_t w = kid_at;
           for (int c = 0; c < k; c++)
             if (give[c]) {
+              if (!GA_IN_BOUNDS(w < kMaxLeavesPerStep && (uint32_t)(first + c) < p.nodes, status)) break;
               f_node[wi][cur ^ 1][w] = first + c;
               f_cnt[wi][cur ^ 1][w] = give[c];
               w++;
@@ -415,7 +419,7 @@ __global__ void __launch_bounds__(32 * kSelectWarps) select_kernel(Pool p, Table
 
 // One thread per leaf: outcomes up the path (score in half points for the
 // player who made the move into each node).
-__global__ void backprop_kernel(Pool p, Table t, Leaves l, uint32_t ppl, uint32_t max_leaves) {
+__global__ void backprop_kernel(Pool p, Table t, Leaves l, uint32_t ppl, uint32_t max_leaves, uint32_t *status) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= max_leaves || i >= l.sizes[0]) return;
   const int32_t s = l.search[i];
@@ -428,6 +432,7 @@ __global__ void backprop_kernel(Pool p, Table t, Leaves l, uint32_t ppl, uint32_
     dr += o == 0;
   }
   for (int32_t n = l.node[i]; n >= 0; n = p.parent[n]) {
+    if (!GA_IN_BOUNDS((uint32_t)n < p.nodes, status)) break;
     const uint32_t mover = (p.board[n].w & 1u) ^ 1u;  // 0: PLAYER_1 moved into n
     atomicAdd(&p.info[n].z, ppl);
     atomicAdd(&p.info[n].w, 2u * (mover == 0 ? w1 : w2) + dr);
@@ -441,7 +446,7 @@ __global__ void backprop_kernel(Pool p, Table t, Leaves l, uint32_t ppl, uint32_
 // leaves: the playouts, which end at once with the exact result), added as
 // kUnits visits.
 __global__ void backprop_learned_kernel(Pool p, Table t, Leaves l, uint32_t ppl, uint32_t max_leaves,
-                                        Learned lrn) {
+                                        Learned lrn, uint32_t *status) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= max_leaves || i >= l.sizes[0]) return;
   const int32_t s = l.search[i];
@@ -459,6 +464,7 @@ __global__ void backprop_learned_kernel(Pool p, Table t, Leaves l, uint32_t ppl,
   const uint32_t s1 = (uint32_t)__float2int_rn(dm::mul((float)kUnits, dm::add(1.0f, x1)));  // half points of PLAYER_1
   const uint32_t s2 = 2u * kUnits - s1;
   for (int32_t n = leaf; n >= 0; n = p.parent[n]) {
+    if (!GA_IN_BOUNDS((uint32_t)n < p.nodes, status)) break;
     const uint32_t mover = (p.board[n].w & 1u) ^ 1u;  // 0: PLAYER_1 moved into n
     atomicAdd(&p.info[n].z, kUnits);
     atomicAdd(&p.info[n].w, mover == 0 ? s1 : s2);
@@ -564,7 +570,7 @@ struct gpuai_searches {
   std::vector<void *> allocations;
   // learned searches
   gpuai_net *net = nullptr;
-  Learned lrn{1.5f, 1.0f};
+  Learned lrn{1.5f, 1.0f, 0u};
   ga::net::Fwd fw;
   cudaStream_t side = nullptr;  // the network's branch of a learned step
   cudaEvent_t fork = nullptr, join = nullptr;
@@ -679,7 +685,7 @@ int enqueue_step(gpuai_searches *s, uint32_t q) {
     b.dev_sizes = s->psizes;
     SCK(launch_playouts(b, s->policy, kPlayoutBlock, s->sms * s->blocks_per_sm, st), "playout kernel launch");
     backprop_learned_kernel<<<(max_leaves + 255) / 256, 256, 0, st>>>(s->pool, s->tab, s->leaves, s->ppl,
-                                                                      max_leaves, s->lrn);
+                                                                      max_leaves, s->lrn, s->ctl + 1);
     SCK(cudaGetLastError(), "search kernel launch");
     return GPUAI_OK;
   }
@@ -701,9 +707,10 @@ int enqueue_step(gpuai_searches *s, uint32_t q) {
   if (s->net) {
     SCK(cudaStreamWaitEvent(st, s->join, 0), "join");
     backprop_learned_kernel<<<(max_leaves + 255) / 256, 256, 0, st>>>(s->pool, s->tab, s->leaves, s->ppl,
-                                                                      max_leaves, s->lrn);
+                                                                      max_leaves, s->lrn, s->ctl + 1);
   } else {
-    backprop_kernel<<<(max_leaves + 255) / 256, 256, 0, st>>>(s->pool, s->tab, s->leaves, s->ppl, max_leaves);
+    backprop_kernel<<<(max_leaves + 255) / 256, 256, 0, st>>>(s->pool, s->tab, s->leaves, s->ppl, max_leaves,
+                                                              s->ctl + 1);
   }
   SCK(cudaGetLastError(), "search kernel launch");
   return GPUAI_OK;
@@ -735,6 +742,8 @@ int gpuai_searches_create(int device, uint32_t max_searches, uint32_t pool_nodes
   s->ppl = playouts_per_leaf;
   s->policy = policy;
   s->seed = seed;
+  s->pool.nodes = pool_nodes;
+  s->lrn.max_leaves = max_leaves_per_step;
   auto fail = [&](int rc) {
     gpuai_searches_destroy(s);
     return rc;
@@ -852,6 +861,7 @@ int gpuai_searches_remove(gpuai_searches *s, int32_t slot) {
 }
 
 int gpuai_searches_step(gpuai_searches *s, uint32_t steps, uint32_t leaves_per_search, int32_t use_graph) {
+  GPUAI_RANGE("gpuai_searches_step");
   if (!s) return err(GPUAI_ERR_INVALID, "gpuai_searches_step: NULL");
   if (leaves_per_search == 0 || leaves_per_search > s->qmax)
     return err(GPUAI_ERR_INVALID, "gpuai_searches_step: leaves_per_search outside 1..max_leaves_per_step");
@@ -886,6 +896,7 @@ int gpuai_searches_step(gpuai_searches *s, uint32_t steps, uint32_t leaves_per_s
 }
 
 int gpuai_searches_poll(gpuai_searches *s, uint64_t *done, uint64_t *budget, uint32_t n, uint32_t *status) {
+  GPUAI_RANGE("gpuai_searches_poll");
   if (!s || !done || !budget) return err(GPUAI_ERR_INVALID, "gpuai_searches_poll: NULL");
   if (n > s->slots) return err(GPUAI_ERR_INVALID, "gpuai_searches_poll: n exceeds max_searches");
   std::lock_guard<std::mutex> lock(s->mu);

@@ -55,13 +55,14 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
 constexpr uint64_t kWaitLimitNs = 1000000000ull;  // 1 s: far above any legitimate wait here
 
 // Waits until the phase of `bar` with parity `parity` has completed.  Returns
-// false (and the caller reports an error) if that takes longer than 1 s.
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
+// false (and the caller reports an error) if that takes longer than limit_ns
+// (1 s unless a caller asks for less).
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, uint64_t limit_ns = kWaitLimitNs) {
   if (mbar_try_wait(bar, parity)) return true;
   const uint64_t t0 = globaltimer();
   for (uint32_t i = 1;; i++) {
     if (mbar_try_wait(bar, parity)) return true;
-    if ((i & 63u) == 0 && globaltimer() - t0 > kWaitLimitNs) return false;
+    if ((i & 63u) == 0 && globaltimer() - t0 > limit_ns) return false;
   }
 }
 

@@ -18,7 +18,9 @@ import numpy as np
 
 PKG = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(PKG)
-LIB_PATH = os.path.join(PKG, "lib", "libgpuai.so")
+# GPUAI_LIB selects another build of the library, e.g. lib/libgpuai_checked.so
+# (the kernels' bounds checks compiled in)
+LIB_PATH = os.environ.get("GPUAI_LIB") or os.path.join(PKG, "lib", "libgpuai.so")
 HEADER = os.path.join(ROOT, "include", "gpuai.h")
 
 POLICY_RANDOM = 0
@@ -121,6 +123,7 @@ def load_library(path: str = LIB_PATH):
     lib.gpuai_playouts_learned.argtypes = [vp, vp, vp, vp, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
                                            ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint32, ctypes.c_float, vp, vp,
                                            vp, vp]
+    lib.gpuai_net_wait_selftest.argtypes = [vp, ctypes.c_uint32, _u32p]
     lib.gpuai_searches_set_proposal.argtypes = [vp, ctypes.c_uint32, ctypes.c_float]
     lib.gpuai_searches_nodes.argtypes = [vp, ctypes.c_int32, ctypes.c_uint32, vp, vp, vp, vp, _u32p]
     lib.gpuai_searches_leaves.argtypes = [vp, ctypes.c_uint32, _u32p, vp, vp, vp, vp, vp, vp, vp]
@@ -474,6 +477,13 @@ class Net:
                                             q.ctypes.data_as(fp), n, tau, value_coef, g.ctypes.data_as(fp),
                                             loss.ctypes.data_as(fp)))
         return g, loss
+
+    def wait_selftest(self, wait_limit_us: int = 2000) -> int:
+        """Status word of a GEMM launched with no loads and a short wait limit
+        (gpuai_net_wait_selftest): bit 16 set when its bounded wait ran out."""
+        st = ctypes.c_uint32()
+        _check(self.lib.gpuai_net_wait_selftest(self.h, wait_limit_us, ctypes.byref(st)))
+        return int(st.value)
 
     def train_step(self, d_boards: int, d_value: int, d_move_q: int, n: int, lr: float, tau: float = 0.1,
                    value_coef: float = 1.0, want_loss: bool = False):

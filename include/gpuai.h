@@ -265,6 +265,15 @@ int gpuai_net_train_step(gpuai_net *net, const gpuai_board *d_boards, const floa
 int gpuai_label_positions(gpuai_ctx *ctx, const gpuai_board *d_pos, uint32_t n, uint32_t playouts_per_position,
                           uint64_t seed, uint64_t stream_base, int32_t policy, float *d_value, float *d_move_q,
                           uint8_t *d_nmoves, void *stream);
+/* Self-test of the tensor-core kernels' bounded waits (no counterpart in the
+ * reference): one tile of the first layer's GEMM is launched with no TMA load
+ * issued and every barrier wait limited to wait_limit_us (1..10^6), so the
+ * MMA warp's wait for its first stage runs out.  The kernel then records the
+ * failure in the status word, frees its tensor memory and returns; *status is
+ * that word (bit 16 set when the wait ran out), cleared afterwards.  The
+ * network stays usable. */
+int gpuai_net_wait_selftest(gpuai_net *net, uint32_t wait_limit_us, uint32_t *status);
+
 /* Learned-proposal playouts (no counterpart in the reference; the shape of its
  * heuristicPlayoutKernel, src/heuristicPlayout.cu:54-88, with the network's
  * policy in place of scoreMove): the first guided_plies plies of every playout

@@ -105,3 +105,14 @@ def test_apply_move_equals_the_oracle(lib_built):
     bad[0] = 40  # from square out of range
     with pytest.raises(E.GpuAIError):
         E.apply_move(boards[0], bad)
+
+
+def test_checked_build_exports_header():
+    """The bounds-checked build (-DGPUAI_CHECKS) compiles and exports the same
+    entry points."""
+    from gpu_ai_gb300.build import build
+    so = build(checks=True)
+    names = E.header_symbols()
+    nm = subprocess.run(["nm", "-D", "--defined-only", so], capture_output=True, text=True).stdout
+    exported = {line.split()[-1] for line in nm.splitlines() if " T " in line}
+    assert set(names) <= exported

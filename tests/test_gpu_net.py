@@ -238,3 +238,22 @@ def test_set_net_rejected_while_searches_run(Net):
         s.set_net(net)
     s.close()
     net.close()
+
+
+def test_bounded_wait_runs_out_cleanly(Net):
+    """A GEMM launched with no TMA load and a 2 ms wait limit: its MMA warp's
+    barrier wait runs out, the kernel reports it in the status word, frees its
+    tensor memory and returns; the network keeps working afterwards (a kernel
+    that kept its TMEM would leave later allocations waiting)."""
+    net = Net(0, max_batch=256, seed=1)
+    p = _params(4)
+    net.set_params(p)
+    for _ in range(2):
+        st = net.wait_selftest(2000)
+        assert st & 16
+    boards, _, _, _ = _positions(7, 200)
+    value, logits = net.forward(boards)
+    ref = mlp.forward(p, boards, emulate=True)
+    assert np.abs(logits - ref["logits"]).max() <= 1e-2 * np.abs(ref["logits"]).max()
+    assert net.wait_selftest(1000) & 16
+    net.close()
