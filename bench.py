@@ -53,6 +53,11 @@ WORKLOAD = {
 # correct kernel's ncu capture (smsp__thread_inst_executed.sum / plies);
 # the algorithmic work unit of the integer-issue roofline.
 OPS_PER_PLY = 260.0
+# Lane instructions per ply of the other two policies' kernels (playout_kernel<1,
+# 256>, playout_kernel<2, 256>), frozen from one ncu capture of the benchmark
+# batch (smsp__thread_inst_executed_pred_on.sum / plies): 12.25e9 / 12.65e6 and
+# 6.66e9 / 15.72e6.
+OPS_PER_PLY_POLICY = {"ref_heuristic": 969.0, "eps_greedy": 424.0}
 # DRAM bytes per launch of the playout kernel from one ncu capture
 # (dram__bytes_read.sum + dram__bytes_write.sum).
 TRAFFIC_BYTES = 47104  # one ncu capture of the benchmark launch: 46.3 KB read, 0.8 KB written
@@ -307,6 +312,9 @@ def run_ours(args):
 
     torch.cuda.set_device(local)
     eng = Engine(local)
+    layouts = {"thread": 0, "warp": 1, "pooled": 2}
+    if args.layout:
+        eng.set_layout(0, layouts[args.layout])
     if args.block:
         eng.set_launch(0, args.block, args.blocks_per_sm)
     info = eng.device_info()
@@ -434,6 +442,11 @@ def run_ours(args):
                 pl_sum += pl
         pols[name] = {"playouts_per_s": len(ts) * TOTAL / sum(ts), "ms_per_step": sum(ts) / len(ts) * 1e3,
                       "plies_per_playout": pl_sum / (len(ts) * TOTAL)}
+        pl_s = pl_sum / sum(ts)
+        ach = pl_s * OPS_PER_PLY_POLICY[name] / 1e12
+        pols[name]["roofline"] = {"bound": "int_issue", "unit": "Tlane-op/s", "ops_per_ply": OPS_PER_PLY_POLICY[name],
+                                  "plies_per_s": pl_s, "achieved": ach, "peak": peak_ops / 1e12,
+                                  "frac": ach / (peak_ops / 1e12)}
     line["policies"] = pols
     # a short timed loop can fall between two 50 ms samples: then the clocks
     # of the whole GPU run (warm-up, timed loops, policy legs) are reported
@@ -611,7 +624,7 @@ def run_train(args):
     both sides); inputs stay resident."""
     from gpu_ai_gb300 import Net
     peaks, peak_kind = measured_peaks()
-    n = 8192
+    n = args.train_batch
     b, z, q = _train_rows(n)
     net = Net(0, max_batch=n, seed=1)
     for _ in range(args.warmup):
@@ -629,7 +642,7 @@ def run_train(args):
         "higher_is_better": True, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": step_s * 1e3, "dtype": "bf16 (fp32 accumulation)",
         "data": "synthetic (seeded positions, random targets)",
-        "config": {"workload": "Adam steps on 8192 positions, 129-256-256-(1024+1)", "batch": n},
+        "config": {"workload": f"Adam steps on {n} positions, 129-256-256-(1024+1)", "batch": n},
         "roofline": {"bound": "tensor", "achieved": tflops, "peak": peaks["bf16_tflops"], "unit": "TFLOP/s",
                      "frac": tflops / peaks["bf16_tflops"], "peak_kind": peak_kind,
                      "flop_per_position": TRAIN_FLOPS_PER_POSITION},
@@ -741,6 +754,8 @@ def main():
                     help="playouts workload: playouts per position (4,096 is the benchmark batch)")
     ap.add_argument("--block", type=int, default=0, help="threads per block of the playout kernel (0: default)")
     ap.add_argument("--blocks-per-sm", type=int, default=0, help="resident blocks per SM (0: as many as fit)")
+    ap.add_argument("--layout", choices=["", "thread", "warp", "pooled"], default="",
+                    help="playout kernel layout of the uniform random policy (default: the library's)")
     ap.add_argument("--workload", choices=["playouts", "mcts", "searches", "serve", "learned", "train",
                                            "learned-search"],
                     default="playouts")
@@ -754,6 +769,7 @@ def main():
                     help="learned workload: plies of every playout drawn from the network's policy")
     ap.add_argument("--temperature", type=float, default=1.0, help="learned workload: proposal temperature")
     ap.add_argument("--save-net", default="", help="learned workload: save the trained network to this file")
+    ap.add_argument("--train-batch", type=int, default=8192, help="train workload: positions per Adam step")
     ap.add_argument("--rate", type=float, default=1000.0, help="serve workload: requests per second")
     ap.add_argument("--serve-leaves", type=int, default=512,
                     help="serve workload: leaves per search per step (1..512; every request gets the same)")

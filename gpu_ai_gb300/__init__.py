@@ -11,6 +11,7 @@ from .engine import (  # noqa: F401
     ERR_OOM,
     LAYOUT_THREAD,
     LAYOUT_WARP,
+    LAYOUT_POOLED,
     OK,
     POLICY_EPS_GREEDY,
     POLICY_RANDOM,
@@ -37,4 +38,5 @@ __all__ = [
     "POLICY_EPS_GREEDY",
     "LAYOUT_THREAD",
     "LAYOUT_WARP",
+    "LAYOUT_POOLED",
 ]

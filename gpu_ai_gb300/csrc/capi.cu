@@ -255,7 +255,7 @@ int gpuai_set_launch(gpuai_ctx *ctx, int32_t policy, int32_t block_threads, int3
 int gpuai_set_layout(gpuai_ctx *ctx, int32_t policy, int32_t layout) {
   if (!ctx) return fail(GPUAI_ERR_INVALID, "gpuai_set_layout: ctx is NULL");
   if (policy < 0 || policy > 2) return fail(GPUAI_ERR_INVALID, "gpuai_set_layout: unknown policy %d", policy);
-  if (layout != GPUAI_LAYOUT_THREAD && layout != GPUAI_LAYOUT_WARP)
+  if (layout != GPUAI_LAYOUT_THREAD && layout != GPUAI_LAYOUT_WARP && layout != GPUAI_LAYOUT_POOLED)
     return fail(GPUAI_ERR_INVALID, "gpuai_set_layout: unknown layout %d", layout);
   if (layout == GPUAI_LAYOUT_WARP && policy != GPUAI_POLICY_RANDOM)
     return fail(GPUAI_ERR_INVALID, "gpuai_set_layout: the warp layout plays the uniform random policy only");

@@ -69,7 +69,30 @@ constexpr int playout_min_blocks() {
   return 65536 / (regs * BLOCK);
 }
 
-template <int POLICY, int BLOCK>
+// Block pool of the pooled layout: a shared-memory lock that lane 0 tries to
+// take once (a warp that does not get it carries on as the unpooled kernel
+// does and tries again on a later iteration: nothing ever waits for it), and
+// the two pools' capacity.
+constexpr uint32_t kPoolCap = 64;
+
+__device__ __forceinline__ bool pool_lock(uint32_t *lock, uint32_t lane) {
+  uint32_t got = 0;
+  if (lane == 0) got = atomicCAS(lock, 0u, 1u) == 0u ? 1u : 0u;
+  got = __shfl_sync(kFull, got, 0);
+  __threadfence_block();
+  __syncwarp();
+  return got != 0;
+}
+
+__device__ __forceinline__ void pool_unlock(uint32_t *lock, uint32_t lane) {
+  __threadfence_block();
+  __syncwarp();
+  if (lane == 0) atomicExch(lock, 0u);
+}
+
+__device__ __forceinline__ uint32_t vload(const uint32_t *p) { return *reinterpret_cast<const volatile uint32_t *>(p); }
+
+template <int POLICY, int BLOCK, bool POOL>
 __global__ void __launch_bounds__(BLOCK, (playout_min_blocks<POLICY, BLOCK>())) playout_kernel(PlayoutArgs a) {
   if (a.dev_sizes != nullptr) {
     a.npos = __ldg(&a.dev_sizes[0]);
@@ -105,18 +128,105 @@ __global__ void __launch_bounds__(BLOCK, (playout_min_blocks<POLICY, BLOCK>())) 
     // into its lowest threads through shared memory; warps left without games
     // wait at the next barrier instead of issuing empty iterations.  The loop
     // ends for the whole block when it has no game left.
+    //
+    // Pooled layout (POOL): while work remains, a lane whose ply must wait for
+    // a men's multi-jump or king capture search hands its game to the block's
+    // pending pool and takes a new one; once the pool holds 32 such games, the
+    // warp that sees it moves its own games to the block's ready pool, takes
+    // the 32 and plays their deferred plies at once with every lane busy.
+    // Free lanes take ready games before new ones (and pending ones once the
+    // work ran out); compaction packs the pools' games too.  A game keeps its
+    // whole state (board, stream, ring of draws) wherever it is played, so
+    // the outcomes are the same as without the pools.
     constexpr int kWords = 17;
+    constexpr uint32_t kCap = POOL ? kPoolCap : 1u;
     __shared__ uint32_t s_slot[kWords][BLOCK];
     __shared__ uint32_t s_cnt[BLOCK / 32];
+    __shared__ uint32_t s_pend[kWords][kCap];   // games waiting for a deferred ply
+    __shared__ uint32_t s_ready[kWords][kCap];  // games a swap moved out of their lane
+    __shared__ uint32_t s_pool[4];              // lock, pending games, ready games
     const uint32_t warp = threadIdx.x >> 5;
+    const uint32_t lt = (1u << lane) - 1u;
+    if constexpr (POOL) {
+      if (threadIdx.x < 4) s_pool[threadIdx.x] = 0;
+      __syncthreads();
+    }
     DrawRing rs;
     rs.start(0, 0, 0);
     uint32_t pend = 0;    // deferred ply: 0 none, 1 men's multi-jump, 2 king capture search
     bool sparse = false;  // warp-uniform: the work ran out and the warp holds kSparseLanes games or fewer
     auto pick = [&](uint32_t n) { return rs.pick(n); };
+    // a game's state in word q of column idx of a [kWords][stride] area
+    auto put = [&](uint32_t *area, uint32_t stride, uint32_t idx) {
+      const uint32_t v[kWords] = {b.p1, b.p2, b.kings, b.meta, j, game_plies, pend,
+                                  rs.a0, rs.a1, rs.a2, rs.a3, rs.b0, rs.b1, rs.b2, rs.b3, rs.k, rs.avail};
+#pragma unroll
+      for (int q = 0; q < kWords; q++) area[q * stride + idx] = v[q];
+    };
+    auto take = [&](const uint32_t *area, uint32_t stride, uint32_t idx) {
+      b.p1 = area[idx]; b.p2 = area[stride + idx]; b.kings = area[2 * stride + idx]; b.meta = area[3 * stride + idx];
+      j = area[4 * stride + idx];
+      game_plies = area[5 * stride + idx];
+      pend = area[6 * stride + idx];
+      rs.start(a.seed, stream_of(a, position_of(a, j), j), 0);  // then the buffered draws and counter
+      rs.a0 = area[7 * stride + idx]; rs.a1 = area[8 * stride + idx]; rs.a2 = area[9 * stride + idx];
+      rs.a3 = area[10 * stride + idx]; rs.b0 = area[11 * stride + idx]; rs.b1 = area[12 * stride + idx];
+      rs.b2 = area[13 * stride + idx]; rs.b3 = area[14 * stride + idx];
+      rs.k = area[15 * stride + idx];
+      rs.avail = area[16 * stride + idx];
+    };
     constexpr uint32_t kRefillMask = POLICY == 2 ? 1u : 3u;
     for (uint32_t it = 0;; ++it) {
+      bool swapped = false;  // warp-uniform: this iteration's games came from the pending pool
+      if constexpr (POOL) {
+        // 32 games wait for their deferred ply and the ready pool has room for
+        // this warp's games: play the 32 in this warp now (checked on the men's
+        // phase iterations only)
+        if (!exhausted && (it & (kMenPeriod - 1u)) == kMenPhase) {
+          uint32_t ok = 0;
+          if (lane == 0) ok = vload(&s_pool[1]) >= 32u && vload(&s_pool[2]) + 32u <= kCap;
+          if (__shfl_sync(kFull, ok, 0) && pool_lock(&s_pool[0], lane)) {
+            const uint32_t npend = vload(&s_pool[1]), nready = vload(&s_pool[2]);
+            const uint32_t hm = __ballot_sync(kFull, have);
+            if (npend >= 32u && nready + (uint32_t)__popc(hm) <= kCap) {
+              if (have) put(&s_ready[0][0], kCap, nready + __popc(hm & lt));
+              take(&s_pend[0][0], kCap, npend - 32u + lane);
+              have = true;
+              if (lane == 0) {
+                s_pool[1] = npend - 32u;
+                s_pool[2] = nready + __popc(hm);
+              }
+              swapped = true;
+            }
+            pool_unlock(&s_pool[0], lane);
+            if (swapped) rs.refill();
+          }
+        }
+      }
       if ((it & kRefillMask) == 0) {
+        if constexpr (POOL) {
+          // free lanes take ready games (and, once the work ran out, pending ones)
+          const uint32_t fm = __ballot_sync(kFull, !have);
+          if (fm) {
+            uint32_t avail = 0;
+            if (lane == 0) avail = vload(&s_pool[2]) + (exhausted ? vload(&s_pool[1]) : 0u);
+            if (__shfl_sync(kFull, avail, 0) && pool_lock(&s_pool[0], lane)) {
+              const uint32_t nr = vload(&s_pool[2]), np = exhausted ? vload(&s_pool[1]) : 0u;
+              const uint32_t rank = __popc(fm & lt), k = min((uint32_t)__popc(fm), nr + np);
+              if (!have && rank < k) {
+                if (rank < nr) take(&s_ready[0][0], kCap, nr - 1u - rank);
+                else take(&s_pend[0][0], kCap, np - 1u - (rank - nr));
+                have = true;
+              }
+              if (lane == 0) {
+                const uint32_t from_r = min(k, nr);
+                s_pool[2] = nr - from_r;
+                if (exhausted) s_pool[1] = np - (k - from_r);
+              }
+              pool_unlock(&s_pool[0], lane);
+            }
+          }
+        }
         if (claim(a, have, j, exhausted, lane)) {
           have = true;
           const uint32_t p = position_of(a, j);
@@ -126,8 +236,9 @@ __global__ void __launch_bounds__(BLOCK, (playout_min_blocks<POLICY, BLOCK>())) 
         }
         if (have) rs.refill();
       }
-      const bool men_ok = sparse || (it & (kMenPeriod - 1u)) == kMenPhase;
-      const bool king_ok = sparse || (it & (king_period(POLICY) - 1u)) == kKingPhase;
+      const bool men_ok = sparse || swapped || (it & (kMenPeriod - 1u)) == kMenPhase;
+      const bool king_ok = sparse || swapped || (it & (king_period(POLICY) - 1u)) == kKingPhase;
+      bool deferred_now = false;  // this iteration's ply was deferred (a candidate for the pending pool)
       do {
         if (!have) break;
         if ((pend == 1u && !men_ok) || (pend == 2u && !king_ok)) break;  // still deferred
@@ -149,6 +260,7 @@ __global__ void __launch_bounds__(BLOCK, (playout_min_blocks<POLICY, BLOCK>())) 
         }
         if (n == kNeedMen || n == kNeedKing) {
           pend = n == kNeedMen ? 1u : 2u;
+          deferred_now = true;
           break;
         }
         pend = 0;
@@ -162,6 +274,25 @@ __global__ void __launch_bounds__(BLOCK, (playout_min_blocks<POLICY, BLOCK>())) 
           a.out[j] = (int8_t)(n == 0 ? ((b.meta & 1u) ? 1 : -1) : 0);  // side to move cannot move: loses
         have = false;
       } while (false);
+      if constexpr (POOL) {
+        // hand deferred games to the pending pool while work remains
+        if (!exhausted && !sparse) {
+          const uint32_t pm = __ballot_sync(kFull, deferred_now);
+          uint32_t room = 0;
+          if (pm && lane == 0) room = vload(&s_pool[1]) < kCap;
+          if (pm && __shfl_sync(kFull, room, 0) && pool_lock(&s_pool[0], lane)) {
+            const uint32_t np = vload(&s_pool[1]);
+            const uint32_t k = min((uint32_t)__popc(pm), kCap - np), rank = __popc(pm & lt);
+            if (deferred_now && rank < k) {
+              put(&s_pend[0][0], kCap, np + rank);
+              have = false;
+              pend = 0;
+            }
+            if (lane == 0) s_pool[1] = np + k;
+            pool_unlock(&s_pool[0], lane);
+          }
+        }
+      }
 
       if ((it & (kCompactPeriod - 1u)) != kCompactPeriod - 1u) {
         if (exhausted) {
@@ -199,31 +330,45 @@ __global__ void __launch_bounds__(BLOCK, (playout_min_blocks<POLICY, BLOCK>())) 
         total += c;
         busy_warps += c ? 1u : 0u;
       }
-      if (total == 0) break;
+      // games still in the pools (stable here: every warp knows the work ran
+      // out, so none pushes, and all are between the two barriers)
+      const uint32_t nr = POOL ? vload(&s_pool[2]) : 0u, np = POOL ? vload(&s_pool[1]) : 0u;
+      if (total + nr + np == 0) break;
       sparse = __popc(m) <= kSparseLanes;
-      if ((total + 31u) / 32u >= busy_warps) continue;  // packing would free no warp
-      if (have) {
-        const uint32_t slot = before + __popc(m & ((1u << lane) - 1u));
-        const uint32_t v[kWords] = {b.p1, b.p2, b.kings, b.meta, j, game_plies, pend,
-                                    rs.a0, rs.a1, rs.a2, rs.a3, rs.b0, rs.b1, rs.b2, rs.b3, rs.k, rs.avail};
+      if (nr + np == 0 && (total + 31u) / 32u >= busy_warps) continue;  // packing would free no warp
+      const uint32_t n_all = min((uint32_t)BLOCK, total + nr + np);  // games the block's lanes hold after packing
+      if (have) put(&s_slot[0][0], BLOCK, before + __popc(m & lt));
+      if constexpr (POOL) {
+        // pool games fill the lanes after the live ones: ready games first
+        const uint32_t t = threadIdx.x;
+        if (t >= total && t < n_all) {
+          const uint32_t e = t - total;
+          uint32_t v[kWords];
+          if (e < nr) {
 #pragma unroll
-        for (int q = 0; q < kWords; q++) s_slot[q][slot] = v[q];
+            for (int q = 0; q < kWords; q++) v[q] = s_ready[q][nr - 1u - e];
+          } else {
+#pragma unroll
+            for (int q = 0; q < kWords; q++) v[q] = s_pend[q][np - 1u - (e - nr)];
+          }
+#pragma unroll
+          for (int q = 0; q < kWords; q++) s_slot[q][t] = v[q];
+        }
       }
       __syncthreads();
-      have = threadIdx.x < total;
-      sparse = total <= warp * 32u + kSparseLanes;  // this warp now holds min(32, total - 32 * warp) games
-      if (have) {
-        const uint32_t t = threadIdx.x;
-        b.p1 = s_slot[0][t]; b.p2 = s_slot[1][t]; b.kings = s_slot[2][t]; b.meta = s_slot[3][t];
-        j = s_slot[4][t];
-        game_plies = s_slot[5][t];
-        pend = s_slot[6][t];
-        rs.start(a.seed, stream_of(a, position_of(a, j), j), 0);  // then the buffered draws and counter
-        rs.a0 = s_slot[7][t]; rs.a1 = s_slot[8][t]; rs.a2 = s_slot[9][t]; rs.a3 = s_slot[10][t];
-        rs.b0 = s_slot[11][t]; rs.b1 = s_slot[12][t]; rs.b2 = s_slot[13][t]; rs.b3 = s_slot[14][t];
-        rs.k = s_slot[15][t];
-        rs.avail = s_slot[16][t];
+      if constexpr (POOL) {
+        // every thread has read the counts (before the barrier above); a
+        // second barrier publishes the new ones before any lane pops again
+        if (threadIdx.x == 0) {
+          const uint32_t moved = n_all - total, from_r = min(moved, nr);
+          s_pool[2] = nr - from_r;
+          s_pool[1] = np - (moved - from_r);
+        }
+        __syncthreads();
       }
+      have = threadIdx.x < n_all;
+      sparse = n_all <= warp * 32u + kSparseLanes;  // this warp now holds min(32, n_all - 32 * warp) games
+      if (have) take(&s_slot[0][0], BLOCK, threadIdx.x);
     }
   }
   if (a.plies != nullptr) {
@@ -492,13 +637,13 @@ __global__ void random_positions_kernel(uint64_t seed, uint32_t n, uint32_t min_
 
 // ---- launchers
 
-template <int POLICY>
+template <int POLICY, bool POOL>
 static const void *kernel_for(int block) {
   switch (block) {
-    case 64: return (const void *)playout_kernel<POLICY, 64>;
-    case 128: return (const void *)playout_kernel<POLICY, 128>;
-    case 512: return (const void *)playout_kernel<POLICY, 512>;
-    default: return (const void *)playout_kernel<POLICY, 256>;
+    case 64: return (const void *)playout_kernel<POLICY, 64, POOL>;
+    case 128: return (const void *)playout_kernel<POLICY, 128, POOL>;
+    case 512: return (const void *)playout_kernel<POLICY, 512, POOL>;
+    default: return (const void *)playout_kernel<POLICY, 256, POOL>;
   }
 }
 
@@ -513,9 +658,14 @@ static const void *warp_kernel_for(int block) {
 
 static const void *playout_fn(int policy, int block, int layout) {
   if (layout == kLayoutWarp) return warp_kernel_for(block);
-  if (policy == 1) return kernel_for<1>(block);
-  if (policy == 2) return kernel_for<2>(block);
-  return kernel_for<0>(block);
+  if (layout == kLayoutPooled) {
+    if (policy == 1) return kernel_for<1, true>(block);
+    if (policy == 2) return kernel_for<2, true>(block);
+    return kernel_for<0, true>(block);
+  }
+  if (policy == 1) return kernel_for<1, false>(block);
+  if (policy == 2) return kernel_for<2, false>(block);
+  return kernel_for<0, false>(block);
 }
 
 bool valid_block(int block) { return block == 64 || block == 128 || block == 256 || block == 512; }

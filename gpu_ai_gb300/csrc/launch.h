@@ -83,9 +83,11 @@ struct ProposalArgs {
 };
 cudaError_t launch_proposal_ply(const ProposalArgs &a, cudaStream_t s);
 
-// Playout layouts: a thread per playout (every policy) or a warp per playout
-// (uniform random policy only; same outcomes).
-constexpr int kLayoutThread = 0, kLayoutWarp = 1;
+// Playout layouts: a thread per playout (every policy), a warp per playout
+// (uniform random policy only), or a thread per playout whose deferred
+// multi-jump plies are gathered in a block pool and played by full warps
+// (every policy); the outcomes are the same in all three.
+constexpr int kLayoutThread = 0, kLayoutWarp = 1, kLayoutPooled = 2;
 
 // Playout kernels are instantiated for blocks of 64, 128, 256 and 512 threads.
 bool valid_block(int block);

@@ -49,6 +49,11 @@ using bf16 = __nv_bfloat16;
 struct gpuai_net {
   int device = 0;
   cudaStream_t stream = nullptr;
+  // the backward pass's second stream: the products and sums off the critical
+  // path (dW3, dW2, the bias gradients, the loss means) overlap the chain
+  // loss -> dZ2 -> dZ1 -> dW1 on `stream`
+  cudaStream_t side = nullptr;
+  cudaEvent_t ev_loss = nullptr, ev_b1 = nullptr, ev_b3 = nullptr, ev_side = nullptr;
   uint32_t rows = 0;  // training batch capacity (multiple of 128)
   std::vector<void *> allocs;
   float *params = nullptr, *adam_m = nullptr, *adam_v = nullptr, *grad = nullptr;
@@ -772,6 +777,25 @@ cudaError_t backward_impl(gpuai_net *net, const gpuai_board *boards, const float
   loss_kernel<<<B / 4, 128, 0, s>>>(boards, z, q, n, B, tau, vcoef, net->fw.logits, net->fw.vraw, net->dZ3,
                                       net->dZ3t, L, net->dv, net->rowloss);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  const uint32_t kb = B / kBK;
+  splits[2] = pick_splits(kb, kSplit3);
+  splits[1] = pick_splits(kb, kSplit2);
+  splits[0] = pick_splits(kb, kSplit1);
+  const cudaStream_t t = net->side;
+  // side stream, after the loss: dW3 partials, db3, dwv, the loss means and dbv
+  if ((e = cudaEventRecord(net->ev_loss, s)) != cudaSuccess) return e;
+  if ((e = cudaStreamWaitEvent(t, net->ev_loss, 0)) != cudaSuccess) return e;
+  Epi b2;
+  b2.flags = kEpiPartial;
+  b2.out_f32 = net->p3;
+  b2.ld_f32 = kH;
+  b2.partial_stride = (uint64_t)kOut * kH;
+  if ((e = gemm(net->mdZ3t, net->mH2t, kOut, kH, kBnB2, kb, splits[2], nullptr, net->status, b2, t)) != cudaSuccess)
+    return e;
+  rowsum_kernel<<<kOut, 256, 0, t>>>(net->dZ3t, B, L, nullptr, net->grad + oB3);
+  rowsum_kernel<<<kH, 256, 0, t>>>(net->H2t, B, L, net->dv, net->grad + oWV);
+  loss_reduce_kernel<<<1, 256, 0, t>>>(net->rowloss, net->dv, n, B, net->loss2, net->grad + oBV);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
   Epi b1;
   b1.flags = kEpiRank1 | kEpiMask | kEpiB16 | kEpiB16T;
   b1.r1_row = net->dv;
@@ -784,6 +808,18 @@ cudaError_t backward_impl(gpuai_net *net, const gpuai_board *boards, const float
   b1.ld_t = L;
   if ((e = gemm(net->mdZ3, net->mW3T, B, kH, kBnB1, kOut / kBK, 1, nullptr, net->status, b1, s)) != cudaSuccess)
     return e;
+  // side stream, after dZ2: dW2 partials and db2
+  if ((e = cudaEventRecord(net->ev_b1, s)) != cudaSuccess) return e;
+  if ((e = cudaStreamWaitEvent(t, net->ev_b1, 0)) != cudaSuccess) return e;
+  Epi b4;
+  b4.flags = kEpiPartial;
+  b4.out_f32 = net->p2;
+  b4.ld_f32 = kH;
+  b4.partial_stride = (uint64_t)kH * kH;
+  if ((e = gemm(net->mdZ2t, net->mH1t, kH, kH, kBnB4, kb, splits[1], nullptr, net->status, b4, t)) != cudaSuccess)
+    return e;
+  rowsum_kernel<<<kH, 256, 0, t>>>(net->dZ2t, B, L, nullptr, net->grad + oB2);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
   Epi b3;
   b3.flags = kEpiMask | kEpiB16T;
   b3.mask = net->fw.H1;
@@ -792,24 +828,12 @@ cudaError_t backward_impl(gpuai_net *net, const gpuai_board *boards, const float
   b3.ld_t = L;
   if ((e = gemm(net->mdZ2, net->mW2T, B, kH, kBnB3, kH / kBK, 1, nullptr, net->status, b3, s)) != cudaSuccess)
     return e;
-  const uint32_t kb = B / kBK;
-  splits[2] = pick_splits(kb, kSplit3);
-  splits[1] = pick_splits(kb, kSplit2);
-  splits[0] = pick_splits(kb, kSplit1);
-  Epi b2;
-  b2.flags = kEpiPartial;
-  b2.out_f32 = net->p3;
-  b2.ld_f32 = kH;
-  b2.partial_stride = (uint64_t)kOut * kH;
-  if ((e = gemm(net->mdZ3t, net->mH2t, kOut, kH, kBnB2, kb, splits[2], nullptr, net->status, b2, s)) != cudaSuccess)
-    return e;
-  Epi b4;
-  b4.flags = kEpiPartial;
-  b4.out_f32 = net->p2;
-  b4.ld_f32 = kH;
-  b4.partial_stride = (uint64_t)kH * kH;
-  if ((e = gemm(net->mdZ2t, net->mH1t, kH, kH, kBnB4, kb, splits[1], nullptr, net->status, b4, s)) != cudaSuccess)
-    return e;
+  // side stream, after dZ1: db1; then the main stream waits for the side's work
+  if ((e = cudaEventRecord(net->ev_b3, s)) != cudaSuccess) return e;
+  if ((e = cudaStreamWaitEvent(t, net->ev_b3, 0)) != cudaSuccess) return e;
+  rowsum_kernel<<<kH, 256, 0, t>>>(net->dZ1t, B, L, nullptr, net->grad + oB1);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  if ((e = cudaEventRecord(net->ev_side, t)) != cudaSuccess) return e;
   Epi b5;
   b5.flags = kEpiPartial;
   b5.out_f32 = net->p1;
@@ -818,12 +842,7 @@ cudaError_t backward_impl(gpuai_net *net, const gpuai_board *boards, const float
   if ((e = gemm(net->mdZ1t, net->mXt, kH, kInPad, kBnB5, kb, splits[0], nullptr, net->status, b5, s)) !=
       cudaSuccess)
     return e;
-  rowsum_kernel<<<kH, 256, 0, s>>>(net->dZ1t, B, L, nullptr, net->grad + oB1);
-  rowsum_kernel<<<kH, 256, 0, s>>>(net->dZ2t, B, L, nullptr, net->grad + oB2);
-  rowsum_kernel<<<kOut, 256, 0, s>>>(net->dZ3t, B, L, nullptr, net->grad + oB3);
-  rowsum_kernel<<<kH, 256, 0, s>>>(net->H2t, B, L, net->dv, net->grad + oWV);
-  loss_reduce_kernel<<<1, 256, 0, s>>>(net->rowloss, net->dv, n, B, net->loss2, net->grad + oBV);
-  return cudaGetLastError();
+  return cudaStreamWaitEvent(s, net->ev_side, 0);
 }
 
 cudaError_t run_adam(gpuai_net *net, uint32_t mode, const uint32_t *splits, float lr, cudaStream_t s) {
@@ -942,6 +961,9 @@ int gpuai_net_create(int device, uint32_t max_batch, uint64_t init_seed, gpuai_n
   net->rows = L;
   auto &A = net->allocs;
   cudaError_t e = cudaStreamCreateWithFlags(&net->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&net->side, cudaStreamNonBlocking);
+  for (cudaEvent_t *ev : {&net->ev_loss, &net->ev_b1, &net->ev_b3, &net->ev_side})
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
   if (e == cudaSuccess) e = dalloc(A, &net->params, kParams);
   if (e == cudaSuccess) e = dalloc(A, &net->adam_m, kParams);
   if (e == cudaSuccess) e = dalloc(A, &net->adam_v, kParams);
@@ -1006,9 +1028,13 @@ void gpuai_net_destroy(gpuai_net *net) {
   if (!net) return;
   cudaSetDevice(net->device);
   if (net->stream) cudaStreamSynchronize(net->stream);
+  if (net->side) cudaStreamSynchronize(net->side);
   for (void *p : net->prop_allocs) cudaFree(p);
   if (net->prop_cur) cudaFree(net->prop_cur);
   for (void *p : net->allocs) cudaFree(p);
+  for (cudaEvent_t ev : {net->ev_loss, net->ev_b1, net->ev_b3, net->ev_side})
+    if (ev) cudaEventDestroy(ev);
+  if (net->side) cudaStreamDestroy(net->side);
   if (net->stream) cudaStreamDestroy(net->stream);
   delete net;
 }

@@ -29,6 +29,7 @@ POLICY_EPS_GREEDY = 2
 
 LAYOUT_THREAD = 0
 LAYOUT_WARP = 1
+LAYOUT_POOLED = 2
 
 OK = 0
 ERR_INVALID = -1

@@ -128,13 +128,16 @@ int gpuai_get_launch(gpuai_ctx *ctx, int32_t policy, int32_t *block_threads, int
                      int32_t *max_blocks_per_sm);
 
 /* Playout layout for `policy`: a thread per playout (GPUAI_LAYOUT_THREAD, the
- * default, every policy) or a warp per playout with one lane per dark square
+ * default, every policy), a warp per playout with one lane per dark square
  * (GPUAI_LAYOUT_WARP, uniform random policy only), the shape of the
- * reference's playoutKernel (src/multiplePlayout.cu:14-52).  Outcomes are the
- * same in both layouts; the autotuner measures which is faster.  Setting a
- * layout resets blocks_per_sm to as many as fit. */
+ * reference's playoutKernel (src/multiplePlayout.cu:14-52), or a thread per
+ * playout whose plies that must search a multi-jump are handed to a block-wide
+ * pool and played by full warps (GPUAI_LAYOUT_POOLED, every policy).  Outcomes
+ * are the same in all layouts; the autotuner measures which is faster.
+ * Setting a layout resets blocks_per_sm to as many as fit. */
 #define GPUAI_LAYOUT_THREAD 0
 #define GPUAI_LAYOUT_WARP 1
+#define GPUAI_LAYOUT_POOLED 2
 int gpuai_set_layout(gpuai_ctx *ctx, int32_t policy, int32_t layout);
 int gpuai_get_layout(gpuai_ctx *ctx, int32_t policy, int32_t *layout);
 
