@@ -574,23 +574,33 @@ def run_serve(args):
     (0-60 random plies), time budgets U(10, 200) ms, continuous batching;
     random playouts, reference-heuristic playouts and learned searches
     (network leaf values and priors, 2 random playouts per leaf) side by side."""
+    import torch
     from gpu_ai_gb300.serve import simulate
     from gpu_ai_gb300 import POLICY_RANDOM, POLICY_REF_HEURISTIC
+    mem = torch.cuda.mem_get_info  # (free, total) of the whole device: this process's peak in use
     res = {}
     q = args.serve_leaves
     for name, pol in (("random", POLICY_RANDOM), ("ref_heuristic", POLICY_REF_HEURISTIC)):
         res[name] = simulate(rate=args.rate, n_requests=args.requests, n_games=10000, budget_ms=(10.0, 200.0),
-                             policy=pol, leaves_per_search=q, playouts_per_leaf=args.playouts_per_leaf)
+                             policy=pol, leaves_per_search=q, playouts_per_leaf=args.playouts_per_leaf,
+                             device_memory=mem)
     net = quick_net(args)
     res["learned"] = simulate(rate=args.rate, n_requests=args.requests, n_games=10000, budget_ms=(10.0, 200.0),
-                              policy=POLICY_RANDOM, leaves_per_search=q, playouts_per_leaf=2, net=net)
+                              policy=POLICY_RANDOM, leaves_per_search=q, playouts_per_leaf=2, net=net,
+                              device_memory=mem)
     res["learned"]["network"] = args.net or "trained here: 1M positions x 1024 playouts, 3 epochs"
+    res["learned_proposal"] = simulate(rate=args.rate, n_requests=args.requests, n_games=10000,
+                                       budget_ms=(10.0, 200.0), policy=POLICY_RANDOM, leaves_per_search=q,
+                                       playouts_per_leaf=2, net=net, guided=args.guided,
+                                       temperature=args.temperature, device_memory=mem)
+    res["learned_proposal"]["guided_plies"] = args.guided
     line = {"metric": "serving: search requests with continuous batching", "unit": "ms",
             "value": res["random"]["latency_ms_p99"], "higher_is_better": False, "n_gpus": 1,
             "data": "synthetic (seeded games, Poisson arrivals)",
             "config": {"workload": f"{args.requests} requests at {args.rate} req/s, budgets U(10,200) ms",
                        "leaves_per_search_per_step": q, "playouts_per_leaf": args.playouts_per_leaf},
-            "random": res["random"], "ref_heuristic": res["ref_heuristic"], "learned": res["learned"]}
+            "random": res["random"], "ref_heuristic": res["ref_heuristic"], "learned": res["learned"],
+            "learned_proposal": res["learned_proposal"]}
     print(json.dumps(line), flush=True)
 
 

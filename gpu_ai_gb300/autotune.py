@@ -1,7 +1,8 @@
 """Autotuner for the playout kernel and the batched-search step.
 
 Sweeps, on the current GPU, (1) the playout kernel's layout (a thread per
-playout, or a warp per playout with one lane per square) x launch shape
+playout, a warp per playout with one lane per square, or a thread per playout
+with the block pool for deferred multi-jump plies) x launch shape
 (threads per block 64-512 x resident blocks per SM) on a batch of random
 playouts and
 (2) the batched-search step's leaves per search and playouts per leaf, and
@@ -20,7 +21,9 @@ import time
 
 import numpy as np
 
-from .engine import LAYOUT_THREAD, LAYOUT_WARP, Engine, Searches
+from .engine import LAYOUT_POOLED, LAYOUT_THREAD, LAYOUT_WARP, Engine, Searches
+
+LAYOUT_NAMES = {LAYOUT_THREAD: "thread", LAYOUT_WARP: "warp", LAYOUT_POOLED: "pooled"}
 
 DEFAULT_CACHE = os.path.join(os.path.expanduser("~"), ".cache", "gpu_ai_gb300", "autotune.json")
 
@@ -41,7 +44,7 @@ def _time_playouts(eng: Engine, pos, reps, repeats: int) -> float:
 
 
 def tune_playouts(eng: Engine, n_pos=64, reps_per_pos=4096, repeats=3, blocks=(64, 128, 256, 512),
-                  layouts=(LAYOUT_THREAD, LAYOUT_WARP)):
+                  layouts=(LAYOUT_THREAD, LAYOUT_WARP, LAYOUT_POOLED)):
     pos = eng.random_positions(2016, n_pos, 0, 30)
     reps = np.full(n_pos, reps_per_pos, np.uint32)
     total = n_pos * reps_per_pos
@@ -54,7 +57,7 @@ def tune_playouts(eng: Engine, n_pos=64, reps_per_pos=4096, repeats=3, blocks=(6
             for per_sm in sorted({max(1, mx // 2), max(1, (3 * mx) // 4), mx}):
                 eng.set_launch(0, block, per_sm)
                 t = _time_playouts(eng, pos, reps, repeats)
-                results.append({"layout": "warp" if layout == LAYOUT_WARP else "thread", "block_threads": block,
+                results.append({"layout": LAYOUT_NAMES[layout], "block_threads": block,
                                 "blocks_per_sm": per_sm, "seconds": t, "playouts_per_s": total / t})
     best = max(results, key=lambda r: r["playouts_per_s"])
     _set(eng, best)
@@ -62,7 +65,8 @@ def tune_playouts(eng: Engine, n_pos=64, reps_per_pos=4096, repeats=3, blocks=(6
 
 
 def _set(eng: Engine, p: dict):
-    eng.set_layout(0, LAYOUT_WARP if p.get("layout") == "warp" else LAYOUT_THREAD)
+    by_name = {v: k for k, v in LAYOUT_NAMES.items()}
+    eng.set_layout(0, by_name.get(p.get("layout"), LAYOUT_THREAD))
     eng.set_launch(0, p["block_threads"], p["blocks_per_sm"])
 
 

@@ -61,7 +61,8 @@ class SearchServer:
     def __init__(self, max_searches: int = 4096, pool_nodes: Optional[int] = None, pool_fraction: float = 0.25,
                  leaves_per_search: int = 64, playouts_per_leaf: int = 8, policy: int = POLICY_RANDOM,
                  seed: int = 0, use_graph: bool = True, steps_per_poll: int = 2, net=None,
-                 value_weight: float = 0.5, c_puct: float = 1.5, searches=None):
+                 value_weight: float = 0.5, c_puct: float = 1.5, searches=None, guided: int = 0,
+                 temperature: float = 1.0):
         """`searches`: an already created search pool with the `Searches`
         interface (try_add / step / poll / best / remove / close) to serve
         from instead of creating one; pool_nodes must then be given."""
@@ -78,6 +79,8 @@ class SearchServer:
                                                                 playouts_per_leaf, policy, seed)
         if net is not None:  # learned searches: network leaf values and move priors
             self.s.set_net(net, value_weight, c_puct)
+            if guided:  # and learned-proposal playouts
+                self.s.set_proposal(guided, temperature)
         self.q = leaves_per_search
         self.ppl = playouts_per_leaf
         self.use_graph = use_graph
@@ -144,9 +147,13 @@ class SearchServer:
 def simulate(rate: float = 1000.0, n_requests: int = 2000, n_games: int = 10000, budget_ms=(10.0, 200.0),
              policy: int = POLICY_RANDOM, seed: int = 1, leaves_per_search: int = 64, playouts_per_leaf: int = 8,
              node_capacity: int = 65536, server: Optional[SearchServer] = None, net=None,
-             value_weight: float = 0.5, c_puct: float = 1.5) -> dict:
+             value_weight: float = 0.5, c_puct: float = 1.5, guided: int = 0, temperature: float = 1.0,
+             device_memory=None) -> dict:
     """Poisson arrivals at `rate` req/s of requests on positions drawn from
-    `n_games` seeded games (0-60 random plies), time budgets U(budget_ms)."""
+    `n_games` seeded games (0-60 random plies), time budgets U(budget_ms).
+    device_memory: a function returning (free, total) bytes of the device
+    (cudaMemGetInfo); when given, the peak device memory in use during the
+    run is reported."""
     from .engine import Engine
     rng = np.random.default_rng(seed)
     games = Engine(0).random_positions(seed, n_games, 0, 60)
@@ -154,9 +161,15 @@ def simulate(rate: float = 1000.0, n_requests: int = 2000, n_games: int = 10000,
     budgets = rng.uniform(budget_ms[0], budget_ms[1], n_requests)
     picks = rng.integers(0, n_games, n_requests)
     srv = server or SearchServer(leaves_per_search=leaves_per_search, playouts_per_leaf=playouts_per_leaf,
-                                 policy=policy, seed=seed, net=net, value_weight=value_weight, c_puct=c_puct)
+                                 policy=policy, seed=seed, net=net, value_weight=value_weight, c_puct=c_puct,
+                                 guided=guided, temperature=temperature)
     srv.t0 = time.perf_counter()
+    peak_used = 0
+    if device_memory is not None:
+        free, total = device_memory()
+        peak_used = total - free
     i = 0
+    pumps = 0
     while i < n_requests or srv.queue or srv.active:
         t = srv.now()
         while i < n_requests and arrivals[i] <= t:
@@ -167,6 +180,10 @@ def simulate(rate: float = 1000.0, n_requests: int = 2000, n_games: int = 10000,
             time.sleep(max(0.0, min(0.002, arrivals[i] - t)) if i < n_requests else 0.0)
             continue
         srv.pump()
+        pumps += 1
+        if device_memory is not None and pumps % 16 == 0:
+            free, total = device_memory()
+            peak_used = max(peak_used, total - free)
     elapsed = srv.now()
     lat = np.array([r.latency for r in srv.done]) * 1e3
     playouts = sum(r.playouts for r in srv.done)
@@ -178,6 +195,8 @@ def simulate(rate: float = 1000.0, n_requests: int = 2000, n_games: int = 10000,
         "peak_tree_bytes": srv.peak_nodes_reserved * srv.node_bytes, "pool_bytes": srv.pool_nodes * srv.node_bytes,
         "steps": srv.steps,
     }
+    if device_memory is not None:
+        out["peak_device_bytes_in_use"] = peak_used
     if server is None:
         srv.close()
     return out

@@ -6,7 +6,7 @@ import json
 import numpy as np
 
 from gpu_ai_gb300 import autotune
-from gpu_ai_gb300.engine import LAYOUT_THREAD, LAYOUT_WARP
+from gpu_ai_gb300.engine import LAYOUT_POOLED, LAYOUT_THREAD, LAYOUT_WARP
 
 
 class FakeEngine:
@@ -33,7 +33,7 @@ class FakeEngine:
 def _fake_time(eng, pos, reps, repeats):
     # fastest: thread layout, 512 threads, 2 blocks per SM
     t = 1.0 + abs(eng.block - 512) / 1024 + (eng.max_per_sm[eng.block] - eng.per_sm) / 16
-    return t + (0.5 if eng.layout == LAYOUT_WARP else 0.0)
+    return t + (0.5 if eng.layout == LAYOUT_WARP else (0.25 if eng.layout == LAYOUT_POOLED else 0.0))
 
 
 def test_sweep_keeps_and_sets_the_fastest(monkeypatch):
@@ -42,7 +42,7 @@ def test_sweep_keeps_and_sets_the_fastest(monkeypatch):
     best, results = autotune.tune_playouts(eng, n_pos=4, reps_per_pos=8, repeats=1)
     shapes = {(r["layout"], r["block_threads"], r["blocks_per_sm"]) for r in results}
     # every layout x block size x {half, three quarters, all} of the resident blocks
-    exp = {(l, b, p) for l in ("thread", "warp") for b, mx in eng.max_per_sm.items()
+    exp = {(l, b, p) for l in ("thread", "warp", "pooled") for b, mx in eng.max_per_sm.items()
            for p in {max(1, mx // 2), max(1, 3 * mx // 4), mx}}
     assert shapes == exp
     assert (best["layout"], best["block_threads"], best["blocks_per_sm"]) == ("thread", 512, 2)
