@@ -75,6 +75,13 @@ struct gpuai_net {
   std::vector<void *> prop_allocs;
   ga::Board *prop_cur = nullptr;
   size_t prop_cur_cap = 0;
+  // the training step as one CUDA graph (for its batch size, tau and value
+  // coefficient): it reads the rows from the staging buffers and the learning
+  // rate and bias corrections from `hyper`
+  cudaGraphExec_t train_graph = nullptr;
+  uint32_t graph_n = 0;
+  float graph_tau = 0.0f, graph_vcoef = 0.0f;
+  float *hyper = nullptr;
   std::mutex mu;
 };
 
@@ -507,6 +514,7 @@ struct AdamArgs {
   const float *p1, *p2, *p3;
   uint32_t s1, s2, s3;    // split-K partial counts of dW1, dW2, dW3
   float lr, bc1, bc2;
+  const float *hyper;     // optional device {lr, bc1, bc2} (the graphed training step), else the fields above
   uint32_t mode;          // 0 update, 1 write the gradient to g_out, 2 refresh the BF16 copies only
   float *g_out;
   bf16 *W1b, *W2b, *W3b, *W2T, *W3T;
@@ -533,11 +541,13 @@ __global__ void adam_kernel(AdamArgs a) {
       a.g_out[i] = g;
       return;
     }
+    const float lr = a.hyper ? a.hyper[0] : a.lr, bc1 = a.hyper ? a.hyper[1] : a.bc1,
+                bc2 = a.hyper ? a.hyper[2] : a.bc2;
     const float m = kBeta1 * a.m[i] + (1.0f - kBeta1) * g;
     const float v = kBeta2 * a.v[i] + (1.0f - kBeta2) * g * g;
     a.m[i] = m;
     a.v[i] = v;
-    w -= a.lr * (m / a.bc1) / (sqrtf(v / a.bc2) + kAdamEps);
+    w -= lr * (m / bc1) / (sqrtf(v / bc2) + kAdamEps);
     a.w[i] = w;
   }
   const bf16 wb = __float2bfloat16_rn(w);
@@ -552,6 +562,14 @@ __global__ void adam_kernel(AdamArgs a) {
     a.W3b[j] = wb;
     a.W3T[c * kOut + r] = wb;
   }
+}
+
+// The step's learning rate and bias corrections into device memory, where the
+// graphed training step's Adam kernel reads them.
+__global__ void hyper_kernel(float *hyper, float lr, float bc1, float bc2) {
+  hyper[0] = lr;
+  hyper[1] = bc1;
+  hyper[2] = bc2;
 }
 
 __global__ void tanh_kernel(const float *x, uint32_t n, float *y) {
@@ -845,8 +863,10 @@ cudaError_t backward_impl(gpuai_net *net, const gpuai_board *boards, const float
   return cudaStreamWaitEvent(s, net->ev_side, 0);
 }
 
-cudaError_t run_adam(gpuai_net *net, uint32_t mode, const uint32_t *splits, float lr, cudaStream_t s) {
+cudaError_t run_adam(gpuai_net *net, uint32_t mode, const uint32_t *splits, float lr, cudaStream_t s,
+                     const float *hyper = nullptr) {
   AdamArgs a;
+  a.hyper = hyper;
   a.w = net->params;
   a.m = net->adam_m;
   a.v = net->adam_v;
@@ -994,6 +1014,7 @@ int gpuai_net_create(int device, uint32_t max_batch, uint64_t init_seed, gpuai_n
   if (e == cudaSuccess) e = dalloc(A, &net->in_boards, L);
   if (e == cudaSuccess) e = dalloc(A, &net->in_z, L);
   if (e == cudaSuccess) e = dalloc(A, &net->in_q, (size_t)L * kMaxMoves);
+  if (e == cudaSuccess) e = dalloc(A, &net->hyper, 4);
   if (e != cudaSuccess) return fail(cuda_err(e, "gpuai_net_create: allocation"));
   e = make_map(&net->mW1, net->W1b, kH, kInPad, kBnF1);
   if (e == cudaSuccess) e = make_map(&net->mW2, net->W2b, kH, kH, kBnF2);
@@ -1029,6 +1050,7 @@ void gpuai_net_destroy(gpuai_net *net) {
   cudaSetDevice(net->device);
   if (net->stream) cudaStreamSynchronize(net->stream);
   if (net->side) cudaStreamSynchronize(net->side);
+  if (net->train_graph) cudaGraphExecDestroy(net->train_graph);
   for (void *p : net->prop_allocs) cudaFree(p);
   if (net->prop_cur) cudaFree(net->prop_cur);
   for (void *p : net->allocs) cudaFree(p);
@@ -1165,10 +1187,39 @@ int gpuai_net_train_step(gpuai_net *net, const gpuai_board *d_boards, const floa
   std::lock_guard<std::mutex> lock(net->mu);
   NCK(cudaSetDevice(net->device), "cudaSetDevice");
   const cudaStream_t s = net->stream;
-  uint32_t splits[3];
-  NCK(backward_impl(net, d_boards, d_value_target, d_move_q, n, tau, value_coef, splits, s), "backward");
+  // The step's ~25 launches are replayed as one CUDA graph: the rows are
+  // staged into the network's own buffers (fixed addresses for the graph),
+  // the learning rate and bias corrections go to device memory, and the
+  // graph is captured again only when the batch size, tau or the value
+  // coefficient change.  Same kernels in the same order: same results.
+  NCK(cudaMemcpyAsync(net->in_boards, d_boards, (size_t)n * sizeof(gpuai_board), cudaMemcpyDeviceToDevice, s),
+      "stage boards");
+  NCK(cudaMemcpyAsync(net->in_z, d_value_target, (size_t)n * sizeof(float), cudaMemcpyDeviceToDevice, s),
+      "stage values");
+  NCK(cudaMemcpyAsync(net->in_q, d_move_q, (size_t)n * kMaxMoves * sizeof(float), cudaMemcpyDeviceToDevice, s),
+      "stage move values");
   net->step++;
-  NCK(run_adam(net, 0, splits, lr, s), "adam");
+  hyper_kernel<<<1, 1, 0, s>>>(net->hyper, lr, (float)(1.0 - std::pow(0.9, (double)net->step)),
+                               (float)(1.0 - std::pow(0.999, (double)net->step)));
+  NCK(cudaGetLastError(), "hyper");
+  if (!net->train_graph || net->graph_n != n || net->graph_tau != tau || net->graph_vcoef != value_coef) {
+    if (net->train_graph) cudaGraphExecDestroy(net->train_graph);
+    net->train_graph = nullptr;
+    cudaGraph_t g = nullptr;
+    uint32_t splits[3];
+    NCK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "begin capture");
+    cudaError_t e = backward_impl(net, net->in_boards, net->in_z, net->in_q, n, tau, value_coef, splits, s);
+    if (e == cudaSuccess) e = run_adam(net, 0, splits, 0.0f, s, net->hyper);
+    const cudaError_t ec = cudaStreamEndCapture(s, &g);
+    if (e == cudaSuccess) e = ec;
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&net->train_graph, g, 0);
+    if (g) cudaGraphDestroy(g);
+    NCK(e, "training step graph");
+    net->graph_n = n;
+    net->graph_tau = tau;
+    net->graph_vcoef = value_coef;
+  }
+  NCK(cudaGraphLaunch(net->train_graph, s), "training step");
   if (loss2) {
     NCK(cudaMemcpyAsync(loss2, net->loss2, 2 * sizeof(float), cudaMemcpyDeviceToHost, s), "D2H");
     return check_status(net);
