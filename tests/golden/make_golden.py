@@ -12,10 +12,15 @@ unmodified sources) and records its outputs:
                       HostHeuristicPlayoutDriver (src/heuristicPlayout.cpp:12-48)
                       win/draw/loss counts, 4096 playouts per position
 
+  playout_golden_heuristic_32k.npz  (--heuristic-32k) the reference's
+                      HostHeuristicPlayoutDriver counts on the same 64
+                      positions with 32,768 playouts each: the larger-count
+                      check of the heuristic policy's distribution
+
 The reference host drivers are run with OMP_NUM_THREADS=1 so the counts are
 reproducible (their rand()/engine state is shared across OpenMP threads).
 
-    OMP_NUM_THREADS=1 python tests/golden/make_golden.py
+    OMP_NUM_THREADS=1 python tests/golden/make_golden.py [--heuristic-32k]
 """
 from __future__ import annotations
 
@@ -66,5 +71,22 @@ def main():
     print("host W/D/L", wdl_host.sum(0), "heuristic W/D/L", wdl_heur.sum(0))
 
 
+def heuristic_32k():
+    ref = L.ref()
+    if ref is None:
+        raise SystemExit("reference sources not available: cannot generate golden fixtures")
+    reps = 32768
+    pos = L.random_positions(CONFIG_SEED, CONFIG_POSITIONS, 0, CONFIG_MAX_PLIES)
+    wdl = np.zeros((CONFIG_POSITIONS, 3), np.int64)
+    for i in range(CONFIG_POSITIONS):  # one position at a time: bounded memory, same engine stream
+        wdl[i] = L.wdl(L.host_heuristic_ref(np.repeat(pos[i:i + 1], reps, axis=0)))
+    np.savez_compressed(os.path.join(HERE, "playout_golden_heuristic_32k.npz"), positions=pos, reps=reps,
+                        seed=CONFIG_SEED, max_plies=CONFIG_MAX_PLIES, wdl_host_heuristic=wdl)
+    print("heuristic 32k W/D/L", wdl.sum(0))
+
+
 if __name__ == "__main__":
-    main()
+    if "--heuristic-32k" in sys.argv:
+        heuristic_32k()
+    else:
+        main()

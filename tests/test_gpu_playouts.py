@@ -155,3 +155,20 @@ def test_set_launch_rejects_bad_shapes(engine):
         engine.set_launch(0, 96, 0)
     with pytest.raises(GpuAIError):
         engine.set_launch(5, 256, 0)
+
+
+@pytest.mark.parametrize("seed", [78, 4079])
+def test_heuristic_frequencies_32k_per_position(engine, seed):
+    """The reference-heuristic policy against the reference's
+    HostHeuristicPlayoutDriver with 32,768 playouts per position (8 times the
+    benchmark count, so a smaller difference of distributions would show),
+    for two seeds."""
+    import os
+    g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden",
+                             "playout_golden_heuristic_32k.npz"))
+    pos = g["positions"]
+    reps = np.full(len(pos), int(g["reps"]), dtype=np.uint32)
+    got = engine.playouts(pos, reps, seed=seed, stream_base=1 << 36, policy=1).reshape(len(pos), -1)
+    mine = np.stack([L.wdl(r) for r in got])
+    ok, det = wdl_agreement(mine, g["wdl_host_heuristic"])
+    assert ok, det
