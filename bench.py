@@ -670,29 +670,40 @@ def run_train(args):
 
 def run_learned_search(args):
     """Learned device searches: 400 searches x 64 leaves per step, 2 playouts
-    per leaf, network forward on every leaf; K eager steps timed."""
+    per leaf, network forward on every leaf; K eager steps timed, without and
+    with learned-proposal playouts (--guided plies drawn from the network)."""
     from gpu_ai_gb300 import Engine, Net, Searches
     eng = Engine(0)
     net = Net(0, max_batch=256, seed=1)
     roots = eng.random_positions(5, 400, 0, 60)
-    s = Searches(400, 400 * 20000, 64, 2, seed=1)
-    s.set_net(net, 0.5, 1.5)
-    for i, r in enumerate(roots):
-        s.add(r, 1 << 40, 20000, i << 40)
-    for _ in range(args.warmup):
-        s.step(1, 64, False)
-    s.poll()
-    t0 = time.perf_counter()
-    s.step(args.steps, 64, False)
-    done, _ = s.poll()
-    el = time.perf_counter() - t0
-    leaves = 400 * 64 * args.steps
+    res = {}
+    for guided in (0, args.guided):
+        s = Searches(400, 400 * 20000, 64, 2, seed=1)
+        s.set_net(net, 0.5, 1.5)
+        if guided:
+            s.set_proposal(guided, args.temperature)
+        for i, r in enumerate(roots):
+            s.add(r, 1 << 40, 20000, i << 40)
+        for _ in range(args.warmup):
+            s.step(1, 64, False)
+        s.poll()
+        t0 = time.perf_counter()
+        s.step(args.steps, 64, False)
+        s.poll()
+        el = time.perf_counter() - t0
+        s.close()
+        res[guided] = {"ms_per_step": el / max(1, args.steps) * 1e3,
+                       "leaf_evaluations_per_s": 400 * 64 * args.steps / el,
+                       "playouts_per_s": 400 * 64 * 2 * args.steps / el}
+    base = res[0]
     print(json.dumps({
-        "metric": "learned search steps", "value": leaves / el, "unit": "leaf evaluations/s",
+        "metric": "learned search steps", "value": base["leaf_evaluations_per_s"], "unit": "leaf evaluations/s",
         "higher_is_better": True, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": el / max(1, args.steps) * 1e3, "dtype": "bf16 network, u32 playouts",
+        "ms_per_step": base["ms_per_step"], "dtype": "bf16 network, u32 playouts",
         "data": "synthetic (seeded positions)",
-        "config": {"workload": "400 searches x 64 leaves/step, 2 playouts/leaf, lambda 0.5"}}), flush=True)
+        "config": {"workload": "400 searches x 64 leaves/step, 2 playouts/leaf, lambda 0.5"},
+        "with_proposal": dict(res[args.guided], guided_plies=args.guided, temperature=args.temperature)}),
+        flush=True)
 
 
 def run_learned(args):

@@ -56,6 +56,12 @@ void MCTSPlayer::move(const Move &m) {
   updateCancelled_ = true;
 }
 
+void MCTSPlayer::setState(const State &s) {
+  std::lock_guard<std::mutex> lock(mu_);
+  tree_ = std::make_unique<GameTree>(s, cfg_.perspective);
+  updateCancelled_ = true;  // a batch in flight was selected on the old tree
+}
+
 void MCTSPlayer::start() {
   if (running_) throw std::logic_error("MCTSPlayer already started");
   running_ = true;

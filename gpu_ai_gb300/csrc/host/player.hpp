@@ -27,6 +27,10 @@ class Player {
   virtual void start() {}
   virtual void stop() {}
   virtual void move(const Move &) {}
+  // The game starts from `s` instead of the standard start (the reference's
+  // players always start from getStartingState()): a searching player roots
+  // its tree there, so that moves passed to move() apply to the right state.
+  virtual void setState(const State &) {}
 };
 
 // Uniformly random legal move (src/player.cpp:13-16), own seeded generator.
@@ -57,6 +61,7 @@ class MCTSPlayer : public Player {
   std::string getName() const override { return "mcts_" + driver_->getName(); }
   Move getMove(const State &, bool verbose = true) override;
   void move(const Move &) override;
+  void setState(const State &) override;
   void start() override;
   void stop() override;
 

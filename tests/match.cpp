@@ -97,7 +97,10 @@ std::unique_ptr<MCTSPlayer> make_player(const std::string &name, const Options &
 }
 
 PlayerId play(State s, Player *p[2], unsigned max_plies) {
-  for (int i = 0; i < 2; i++) p[i]->start();
+  for (int i = 0; i < 2; i++) {
+    p[i]->setState(s);  // both trees at the game's start position, the one not to move included
+    p[i]->start();
+  }
   unsigned plies = 0;
   while (!s.isGameOver() && plies < max_plies) {
     const Move m = p[s.turn()]->getMove(s, false);
