@@ -8,7 +8,8 @@
 //
 //   quota_kernel     leaf slots per search this step (min(Q, remaining
 //                    budget)), prefix sums, total leaves / playouts
-//   select_kernel    one warp per search: the step's Q leaf slots are split
+//   select_kernel    a warp per search (a block for steps of 128 leaves or
+//                    more): the step's Q leaf slots are split
 //                    over the tree level by level the way the reference's
 //                    GameTree::select splits a batch (src/mcts.cpp:63-157):
 //                    untried children share the slots equally, otherwise in
@@ -61,8 +62,9 @@ namespace {
 constexpr uint32_t kExpanded = 1u, kTerminal = 2u, kEvaluated = 4u;  // node state bits (info.y >> 16)
 constexpr int kMaxSelectDepth = 512;
 constexpr uint32_t kStatusSelectDepth = 8u;
-constexpr uint32_t kSelectWarps = 4;   // searches per select block
-constexpr uint32_t kMaxLeavesPerStep = 512;  // frontier capacity per search (32 KB of static smem per select block)
+constexpr int kSelectThreads = 128;   // threads per select block: 4 searches of a warp each, or one wide search
+constexpr uint32_t kWideLeaves = 128;  // steps of this many leaves per search or more select with a team of 128
+constexpr uint32_t kMaxLeavesPerStep = 512;  // frontier capacity per search (4 KB of shared memory each)
 constexpr float kUcbC = 1.41421356f;
 constexpr int kMaxChildren = 64;  // moves per position handled by split_slots
 constexpr uint32_t kUnits = 64;   // learned searches: visit units per leaf slot (score2 = units * (1 + value))
@@ -286,46 +288,101 @@ __device__ int split_puct(const Pool &p, int32_t n, int32_t first, int k, uint32
   return kids;
 }
 
-// One warp per search.  The frontier holds (node, slots) pairs; each round
-// every lane takes frontier entries, expands or splits them, and the warp
-// compacts the children it produced into the next frontier and the leaf
-// slots it produced into the search's output range.
-template <bool LEARNED>
-__global__ void __launch_bounds__(32 * kSelectWarps) select_kernel(Pool p, Table t, Leaves l, uint32_t slots,
-                                                                   uint32_t ppl, Learned lrn, uint32_t *status) {
-  __shared__ int32_t f_node[kSelectWarps][2][kMaxLeavesPerStep];
-  __shared__ uint32_t f_cnt[kSelectWarps][2][kMaxLeavesPerStep];
-  const uint32_t lane = threadIdx.x & 31u, wi = threadIdx.x >> 5;
-  const uint32_t s = blockIdx.x * kSelectWarps + wi;
-  if (s >= slots) return;
+// A team of TEAM threads per search (a warp, or the whole 128-thread block
+// for wide steps).  The frontier holds (node, slots) pairs; each round the
+// team takes TEAM frontier entries at a time, expands or splits them, and
+// compacts the children it produced into the next frontier and the leaf slots
+// it produced into the search's output range, in entry order.
+template <bool LEARNED, int TEAM>
+__global__ void __launch_bounds__(kSelectThreads) select_kernel(Pool p, Table t, Leaves l, uint32_t slots,
+                                                                uint32_t ppl, Learned lrn, uint32_t *status) {
+  static_assert(TEAM == 32 || TEAM == kSelectThreads, "a team is a warp or the whole block");
+  constexpr int kTeams = kSelectThreads / TEAM, kWarps = TEAM / 32;
+  __shared__ int32_t f_node[kTeams][2][kMaxLeavesPerStep];
+  __shared__ uint32_t f_cnt[kTeams][2][kMaxLeavesPerStep];
+  __shared__ uint32_t s_scan[kTeams][2][kWarps];
+  const uint32_t lane = threadIdx.x & 31u, tl = threadIdx.x % TEAM, wt = tl >> 5, ti = threadIdx.x / TEAM;
+  const uint32_t s = blockIdx.x * kTeams + ti;
+  if (s >= slots) return;  // uniform over the team
   const int32_t root = t.root[s];
   if (root < 0) return;
   const uint32_t off = t.quota_off[s], q = t.quota_off[s + 1] - off;
   if (q == 0) return;
+  auto team_sync = [&]() {
+    if (TEAM == 32) __syncwarp();
+    else __syncthreads();
+  };
+  // inclusive prefix sums of a and b over the team's threads, and their totals
+  auto scan2 = [&](uint32_t &a, uint32_t &b, uint32_t &ta, uint32_t &tb) {
+    for (uint32_t o = 1; o < 32; o <<= 1) {
+      const uint32_t x = __shfl_up_sync(0xffffffffu, a, o), y = __shfl_up_sync(0xffffffffu, b, o);
+      if (lane >= o) {
+        a += x;
+        b += y;
+      }
+    }
+    if (TEAM == 32) {
+      ta = __shfl_sync(0xffffffffu, a, 31);
+      tb = __shfl_sync(0xffffffffu, b, 31);
+      return;
+    }
+    if (lane == 31) {
+      s_scan[ti][0][wt] = a;
+      s_scan[ti][1][wt] = b;
+    }
+    __syncthreads();
+    uint32_t pa = 0, pb = 0;
+    ta = 0;
+    tb = 0;
+#pragma unroll
+    for (int w = 0; w < kWarps; w++) {
+      const uint32_t va = s_scan[ti][0][w], vb = s_scan[ti][1][w];
+      if ((uint32_t)w < wt) {
+        pa += va;
+        pb += vb;
+      }
+      ta += va;
+      tb += vb;
+    }
+    a += pa;
+    b += pb;
+    __syncthreads();  // s_scan is reused by the next scan
+  };
+  auto team_max = [&](uint32_t x) -> uint32_t {
+    x = __reduce_max_sync(0xffffffffu, x);
+    if (TEAM == 32) return x;
+    if (lane == 0) s_scan[ti][0][wt] = x;
+    __syncthreads();
+    uint32_t m = 0;
+#pragma unroll
+    for (int w = 0; w < kWarps; w++) m = max(m, s_scan[ti][0][w]);
+    __syncthreads();
+    return m;
+  };
   int cur = 0;
   uint32_t nf = 1, emitted = 0;
   int32_t node_next = t.node_next[s];
   const int32_t node_end = t.node_end[s];
-  if (lane == 0) {
-    f_node[wi][0][0] = root;
-    f_cnt[wi][0][0] = q;
+  if (tl == 0) {
+    f_node[ti][0][0] = root;
+    f_cnt[ti][0][0] = q;
   }
-  __syncwarp();
+  team_sync();
   for (int depth = 0; nf > 0; depth++) {
     if (depth >= kMaxSelectDepth) {
-      if (lane == 0) atomicOr(status, kStatusSelectDepth);
+      if (tl == 0) atomicOr(status, kStatusSelectDepth);
       break;
     }
     uint32_t next_n = 0;
-    for (uint32_t base = 0; base < nf; base += 32) {
-      const uint32_t e = base + lane;
-      // pass 1: what each lane's entry produces (children entries or leaf slots)
+    for (uint32_t base = 0; base < nf; base += TEAM) {
+      const uint32_t e = base + tl;
+      // pass 1: what each thread's entry produces (children entries or leaf slots)
       int32_t n = -1, first = 0, k = 0;
       uint32_t T = 0, leaf = 0, kids = 0, visits = 0, score2 = 0, st = 0;
-      int grow = 0;  // children this lane's node gets if it is expanded now
+      int grow = 0;  // children this thread's node gets if it is expanded now
       if (e < nf) {
-        n = f_node[wi][cur][e];
-        T = f_cnt[wi][cur][e];
+        n = f_node[ti][cur][e];
+        T = f_cnt[ti][cur][e];
         const uint4 inf = p.info[n];
         st = inf.y >> 16;
         visits = inf.z;
@@ -345,15 +402,13 @@ __global__ void __launch_bounds__(32 * kSelectWarps) select_kernel(Pool p, Table
           }
         }
       }
-      // node indices for this round's expansions, in lane order; an expansion
-      // that does not fit the search's node range plays out instead
-      uint32_t gx = (uint32_t)grow;
-      for (uint32_t o = 1; o < 32; o <<= 1) {
-        const uint32_t a = __shfl_up_sync(0xffffffffu, gx, o);
-        if (lane >= o) gx += a;
-      }
+      // node indices for this round's expansions, in entry order; an
+      // expansion that does not fit the search's node range plays out
+      // instead (fitting is a prefix of the entries: the inclusive sums grow)
+      uint32_t gx = (uint32_t)grow, unused = 0, gtot = 0, utot = 0;
+      scan2(gx, unused, gtot, utot);
       const bool fits = grow > 0 && node_next + (int32_t)gx <= node_end;
-      const uint32_t fit_end = __reduce_max_sync(0xffffffffu, fits ? gx : 0u);
+      const uint32_t fit_end = team_max(fits ? gx : 0u);
       if (fits && GA_IN_BOUNDS(node_next + (int32_t)gx <= node_end && (uint32_t)node_end <= p.nodes, status)) {
         first = node_next + (int32_t)gx - grow;
         k = grow;
@@ -362,26 +417,20 @@ __global__ void __launch_bounds__(32 * kSelectWarps) select_kernel(Pool p, Table
         leaf = T;
       }
       node_next += (int32_t)fit_end;
-      uint32_t give[kMaxChildren];  // this lane's split, written to the next frontier in pass 2
+      uint32_t give[kMaxChildren];  // this thread's split, written to the next frontier in pass 2
       if (e < nf && !leaf) {
         if (LEARNED)
           kids = (uint32_t)split_puct(p, n, first, k, visits, score2, st, T, lrn.c_puct, give);
         else
           kids = (uint32_t)split_slots(p, first, k, visits, T, give);
       }
-      __syncwarp();
-      // warp prefix sums of children entries and leaf slots
-      uint32_t kx = kids, lx = leaf;
-      for (uint32_t o = 1; o < 32; o <<= 1) {
-        const uint32_t a = __shfl_up_sync(0xffffffffu, kx, o), b2 = __shfl_up_sync(0xffffffffu, lx, o);
-        if (lane >= o) {
-          kx += a;
-          lx += b2;
-        }
-      }
+      team_sync();
+      // team prefix sums of children entries and leaf slots
+      uint32_t kx = kids, lx = leaf, ktot = 0, ltot = 0;
+      scan2(kx, lx, ktot, ltot);
       const uint32_t kid_at = next_n + kx - kids, leaf_at = emitted + lx - leaf;
-      next_n += __shfl_sync(0xffffffffu, kx, 31);
-      emitted += __shfl_sync(0xffffffffu, lx, 31);
+      next_n += ktot;
+      emitted += ltot;
       // pass 2: write children entries and leaf slots
       if (e < nf) {
         if (leaf) {
@@ -398,23 +447,23 @@ __global__ void __launch_bounds__(32 * kSelectWarps) select_kernel(Pool p, Table
           for (int c = 0; c < k; c++)
             if (give[c]) {
               if (!GA_IN_BOUNDS(w < kMaxLeavesPerStep && (uint32_t)(first + c) < p.nodes, status)) break;
-              f_node[wi][cur ^ 1][w] = first + c;
-              f_cnt[wi][cur ^ 1][w] = give[c];
+              f_node[ti][cur ^ 1][w] = first + c;
+              f_cnt[ti][cur ^ 1][w] = give[c];
               w++;
             }
         }
       }
-      __syncwarp();
+      team_sync();
     }
     cur ^= 1;
     nf = next_n;
   }
-  if (lane == 0) t.node_next[s] = node_next;
+  if (tl == 0) t.node_next[s] = node_next;
   // per-slot random streams, in slot order
   const unsigned long long sbase = t.stream_next[s];
-  for (uint32_t i = lane; i < q; i += 32) l.stream[off + i] = sbase + (unsigned long long)i * ppl;
-  __syncwarp();
-  if (lane == 0) t.stream_next[s] = sbase + (unsigned long long)q * ppl;
+  for (uint32_t i = tl; i < q; i += TEAM) l.stream[off + i] = sbase + (unsigned long long)i * ppl;
+  team_sync();
+  if (tl == 0) t.stream_next[s] = sbase + (unsigned long long)q * ppl;
 }
 
 // One thread per leaf: outcomes up the path (score in half points for the
@@ -615,13 +664,26 @@ int enqueue_step(gpuai_searches *s, uint32_t q) {
   // until poll reads them
   SCK(cudaMemsetAsync(s->ctl, 0, sizeof(uint32_t), st), "reset work counter");
   quota_kernel<<<1, 1024, 0, st>>>(s->tab, s->slots, q, s->ppl, s->leaves);
-  const uint32_t sel_blocks = (s->slots + kSelectWarps - 1) / kSelectWarps;
-  if (s->net)
-    select_kernel<true><<<sel_blocks, 32 * kSelectWarps, 0, st>>>(s->pool, s->tab, s->leaves, s->slots, s->ppl,
-                                                                   s->lrn, s->ctl + 1);
-  else
-    select_kernel<false><<<sel_blocks, 32 * kSelectWarps, 0, st>>>(s->pool, s->tab, s->leaves, s->slots, s->ppl,
+  // narrow steps: a warp per search, four per block; wide steps (>= 128 leaves
+  // per search): the whole block per search, 128 frontier entries per round
+  const bool wide = q >= kWideLeaves;
+  const uint32_t per_block = wide ? 1u : (uint32_t)(kSelectThreads / 32);
+  const uint32_t sel_blocks = (s->slots + per_block - 1) / per_block;
+  if (s->net) {
+    if (wide)
+      select_kernel<true, kSelectThreads><<<sel_blocks, kSelectThreads, 0, st>>>(s->pool, s->tab, s->leaves,
+                                                                               s->slots, s->ppl, s->lrn, s->ctl + 1);
+    else
+      select_kernel<true, 32><<<sel_blocks, kSelectThreads, 0, st>>>(s->pool, s->tab, s->leaves, s->slots, s->ppl,
                                                                     s->lrn, s->ctl + 1);
+  } else {
+    if (wide)
+      select_kernel<false, kSelectThreads><<<sel_blocks, kSelectThreads, 0, st>>>(s->pool, s->tab, s->leaves,
+                                                                                s->slots, s->ppl, s->lrn, s->ctl + 1);
+    else
+      select_kernel<false, 32><<<sel_blocks, kSelectThreads, 0, st>>>(s->pool, s->tab, s->leaves, s->slots,
+                                                                     s->ppl, s->lrn, s->ctl + 1);
+  }
   PlayoutArgs a;
   a.pos = reinterpret_cast<const Board *>(s->leaves.board);
   a.offsets = nullptr;

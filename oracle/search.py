@@ -12,7 +12,8 @@ every search's tree, so that a GPU test can compare the trees node for node:
              children share them equally, otherwise in proportion to UCB1
              weights rounded down, the rest one each to the heaviest children
              (first on ties).  The frontier is handled in chunks of 32 entries
-             (one warp's lanes); a chunk's expansions take node indices in
+             (one warp's lanes; 128, the whole block, on steps of 128 leaves
+             per search or more); a chunk's expansions take node indices in
              entry order, and an expansion whose inclusive prefix of children
              would pass the search's node range plays out instead;
   playouts   slot i of a search's step uses random streams stream_next + i * ppl
@@ -55,6 +56,7 @@ MAX_CHILDREN = 64
 UNITS = 64
 PRIORS = 32
 TERMINAL_LEAF = F(2.0)
+WIDE_LEAVES, WIDE_TEAM = 128, 128  # steps of 128+ leaves per search: a 128-thread team per search
 
 
 def _cf(bits: int) -> np.float32:
@@ -299,15 +301,17 @@ class SearchesOracle:
             qs.append(q)
         return qs
 
-    def select(self, s: Search, q: int):
-        """select_kernel for one search: list of leaf node indices in emission order."""
+    def select(self, s: Search, q: int, team: int = 32):
+        """select_kernel for one search: list of leaf node indices in emission
+        order.  `team`: frontier entries handled per round (32, a warp, or 128,
+        the block the kernel gives a search on steps of 128 leaves or more)."""
         learned = self.learned is not None
         leaves = []
         frontier = [(0, q)]
         while frontier:
             nxt = []
-            for base in range(0, len(frontier), 32):
-                chunk = frontier[base:base + 32]
+            for base in range(0, len(frontier), team):
+                chunk = frontier[base:base + team]
                 ent = []
                 for n, T in chunk:
                     nd = s.nodes[n]
@@ -361,11 +365,12 @@ class SearchesOracle:
         playouts per leaf), when given, stands in for the replayed playouts
         (learned-proposal playouts, whose parity is checked on their own)."""
         qs = self.quota(Q)
+        team = WIDE_TEAM if Q >= WIDE_LEAVES else 32
         slots = []
         for si, (s, q) in enumerate(zip(self.slots, qs)):
             if s is None or q == 0:
                 continue
-            leaves = self.select(s, q)
+            leaves = self.select(s, q, team)
             assert len(leaves) == q
             for i, n in enumerate(leaves):
                 slots.append([si, n, s.nodes[n].board, s.stream_next + i * self.ppl, None])

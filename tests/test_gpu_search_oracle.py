@@ -95,6 +95,17 @@ def test_playouts_per_leaf_and_node_range_limits():
          steps=30)
 
 
+def test_wide_steps_block_per_search():
+    """Steps of 128 and 512 leaves per search, where a whole block selects for
+    one search (128 frontier entries per round), with a node range that runs
+    out in the middle of a round."""
+    roots = list(L.random_positions(26, 3, 0, 30))
+    _run(policy=0, ppl=2, q=128, budgets=[6000, 4000, 2000], caps=[150, 12000, 12000], roots=roots, graph=True,
+         steps=30)
+    _run(policy=0, ppl=1, q=512, budgets=[8000, 5000, 3000], caps=[700, 20000, 20000], roots=roots, graph=False,
+         steps=30)
+
+
 @pytest.mark.parametrize("policy", [1, 2])
 def test_other_playout_policies(policy):
     roots = list(L.random_positions(23 + policy, 3, 10, 40))
@@ -114,14 +125,14 @@ def _peaky_params(seed):
     return mlp.pack(d).astype(np.float32)
 
 
-@pytest.mark.parametrize("ppl,graph,guided", [(2, True, 0), (1, False, 0), (2, True, 3)])
-def test_learned_searches_node_for_node(ppl, graph, guided):
+@pytest.mark.parametrize("ppl,graph,guided,q", [(2, True, 0, 32), (1, False, 0, 32), (2, True, 3, 32),
+                                                (1, True, 0, 128)])
+def test_learned_searches_node_for_node(ppl, graph, guided, q):
     """PUCT split with the network's priors, expansion once evaluated, and the
     blended leaf value, with a fixed network; with guided plies the playouts
     are learned-proposal playouts (their outcomes are taken from the GPU: the
     proposal playouts are replayed on their own in test_gpu_proposal.py)."""
     from gpu_ai_gb300 import Net, Searches
-    q = 32
     params = _peaky_params(5)
     net = Net(0, max_batch=256, seed=1)
     net.set_params(params)
