@@ -175,6 +175,33 @@ __global__ void __launch_bounds__(BLOCK, (playout_min_blocks<POLICY, BLOCK>())) 
       rs.k = area[15 * stride + idx];
       rs.avail = area[16 * stride + idx];
     };
+    // Claim order (equal repetitions, at most BLOCK positions): lanes take
+    // the playouts of positions with more pieces first.  Their games are
+    // longer on average, so the last claims of the batch are the shorter
+    // games and less of the batch tail waits on a game that started late.
+    // Playout j keeps its index (its outcome slot and random stream); only the
+    // order in which lanes take the playouts changes.
+    __shared__ uint16_t s_order[BLOCK];
+    __shared__ uint8_t s_key[BLOCK];
+    const bool ordered = a.offsets == nullptr && a.npos > 1 && a.npos <= (uint32_t)BLOCK;
+    if (ordered) {  // uniform over the block
+      const uint32_t t = threadIdx.x;
+      if (t < a.npos) {
+        const Board pb = load_board(a.pos + t);
+        s_key[t] = (uint8_t)popc(pb.p1 | pb.p2);
+      }
+      __syncthreads();
+      if (t < a.npos) {
+        const uint32_t kt = s_key[t];
+        uint32_t rank = 0;
+        for (uint32_t u = 0; u < a.npos; u++) {
+          const uint32_t ku = s_key[u];
+          rank += (ku > kt || (ku == kt && u < t)) ? 1u : 0u;
+        }
+        s_order[rank] = (uint16_t)t;
+      }
+      __syncthreads();
+    }
     constexpr uint32_t kRefillMask = POLICY == 2 ? 1u : 3u;
     for (uint32_t it = 0;; ++it) {
       bool swapped = false;  // warp-uniform: this iteration's games came from the pending pool
@@ -229,6 +256,10 @@ __global__ void __launch_bounds__(BLOCK, (playout_min_blocks<POLICY, BLOCK>())) 
         }
         if (claim(a, have, j, exhausted, lane)) {
           have = true;
+          if (ordered) {  // claim index -> playout index
+            const uint32_t k = j / a.uniform_reps;
+            j = (uint32_t)s_order[k] * a.uniform_reps + (j - k * a.uniform_reps);
+          }
           const uint32_t p = position_of(a, j);
           if (GA_IN_BOUNDS(p < a.npos, a.status)) b = load_board(a.pos + p);
           rs.start(a.seed, stream_of(a, p, j), 0);
