@@ -120,10 +120,10 @@ __global__ void __launch_bounds__(BLOCK, (playout_min_blocks<POLICY, BLOCK>())) 
     // to every kMenPeriod-th and every king_period(POLICY)-th iteration, so
     // that the lanes needing that code run it together and the other
     // iterations stay branch-free.
-    // Once the work counter is exhausted, a warp with kSparseLanes or fewer
+    // Once the work counter is exhausted, a warp with sparse_lanes(POLICY) or fewer
     // games defers nothing: its few games are latency-bound.
     //
-    // Once the work counter is exhausted, every kCompactPeriod-th iteration the
+    // Once the work counter is exhausted, every compact_period(POLICY)-th iteration the
     // block packs its unfinished games (board, random-stream state, counters)
     // into its lowest threads through shared memory; warps left without games
     // wait at the next barrier instead of issuing empty iterations.  The loop
@@ -154,7 +154,9 @@ __global__ void __launch_bounds__(BLOCK, (playout_min_blocks<POLICY, BLOCK>())) 
     DrawRing rs;
     rs.start(0, 0, 0);
     uint32_t pend = 0;    // deferred ply: 0 none, 1 men's multi-jump, 2 king capture search
-    bool sparse = false;  // warp-uniform: the work ran out and the warp holds kSparseLanes games or fewer
+    bool sparse = false;  // warp-uniform: the work ran out and the warp holds sparse_lanes(POLICY) games or fewer
+    constexpr uint32_t kCompactPeriod = compact_period(POLICY);
+    constexpr uint32_t kSparseLanes = sparse_lanes(POLICY);
     auto pick = [&](uint32_t n) { return rs.pick(n); };
     // a game's state in word q of column idx of a [kWords][stride] area
     auto put = [&](uint32_t *area, uint32_t stride, uint32_t idx) {
@@ -346,7 +348,7 @@ __global__ void __launch_bounds__(BLOCK, (playout_min_blocks<POLICY, BLOCK>())) 
         exhausted = true;
       }
       // Only warps that know the work is exhausted get here; they all pass the
-      // same sequence of compaction points (it % kCompactPeriod equal, absolute
+      // same sequence of compaction points (it % compact_period equal, absolute
       // iteration counts may differ).  This barrier also keeps a fast warp from
       // writing s_cnt for the next point while a slow one still reads it.
       __syncthreads();

@@ -32,7 +32,11 @@ __device__ __forceinline__ bool ga_in_bounds(bool ok, uint32_t *status) {
 
 constexpr int kPlayoutBlock = 256;        // default threads per block
 constexpr uint32_t kMaxPlies = 4096;
-constexpr uint32_t kCompactPeriod = 16;   // iterations between block compactions once the work runs out (power of 2, >= 4)
+// Iterations between block compactions once the work runs out (a power of 2,
+// >= 4): 16 for the uniform random policy, 8 for the other two, whose plies
+// are longer (measured: 8 is 1.2-1.7 % faster for them, 1.5 % slower for the
+// uniform policy on the benchmark batch).
+GA_HD constexpr uint32_t compact_period(int policy) { return policy == 0 ? 16u : 8u; }
 
 struct PlayoutArgs {
   const Board *pos;
