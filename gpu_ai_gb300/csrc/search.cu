@@ -62,8 +62,11 @@ namespace {
 constexpr uint32_t kExpanded = 1u, kTerminal = 2u, kEvaluated = 4u;  // node state bits (info.y >> 16)
 constexpr int kMaxSelectDepth = 512;
 constexpr uint32_t kStatusSelectDepth = 8u;
-constexpr int kSelectThreads = 128;   // threads per select block: 4 searches of a warp each, or one wide search
-constexpr uint32_t kWideLeaves = 128;  // steps of this many leaves per search or more select with a team of 128
+constexpr int kSelectThreads = 128;   // threads per narrow select block: 4 searches of a warp each
+constexpr uint32_t kWideLeaves = 128;  // steps of this many leaves per search or more select with a block per search
+// Team size of a step with Q leaves per search: a warp below kWideLeaves,
+// else a block of 128, 256 or 512 threads (the largest power of two <= Q).
+inline int select_team(uint32_t Q) { return Q < kWideLeaves ? 32 : (Q < 256 ? 128 : (Q < 512 ? 256 : 512)); }
 constexpr uint32_t kMaxLeavesPerStep = 512;  // frontier capacity per search (4 KB of shared memory each)
 constexpr float kUcbC = 1.41421356f;
 constexpr int kMaxChildren = 64;  // moves per position handled by split_slots
@@ -294,10 +297,10 @@ __device__ int split_puct(const Pool &p, int32_t n, int32_t first, int k, uint32
 // compacts the children it produced into the next frontier and the leaf slots
 // it produced into the search's output range, in entry order.
 template <bool LEARNED, int TEAM>
-__global__ void __launch_bounds__(kSelectThreads) select_kernel(Pool p, Table t, Leaves l, uint32_t slots,
-                                                                uint32_t ppl, Learned lrn, uint32_t *status) {
-  static_assert(TEAM == 32 || TEAM == kSelectThreads, "a team is a warp or the whole block");
-  constexpr int kTeams = kSelectThreads / TEAM, kWarps = TEAM / 32;
+__global__ void __launch_bounds__(TEAM == 32 ? kSelectThreads : TEAM)
+    select_kernel(Pool p, Table t, Leaves l, uint32_t slots, uint32_t ppl, Learned lrn, uint32_t *status) {
+  static_assert(TEAM == 32 || TEAM == 128 || TEAM == 256 || TEAM == 512, "a team is a warp or a whole block");
+  constexpr int kTeams = TEAM == 32 ? kSelectThreads / 32 : 1, kWarps = TEAM / 32;
   __shared__ int32_t f_node[kTeams][2][kMaxLeavesPerStep];
   __shared__ uint32_t f_cnt[kTeams][2][kMaxLeavesPerStep];
   __shared__ uint32_t s_scan[kTeams][2][kWarps];
@@ -664,25 +667,30 @@ int enqueue_step(gpuai_searches *s, uint32_t q) {
   // until poll reads them
   SCK(cudaMemsetAsync(s->ctl, 0, sizeof(uint32_t), st), "reset work counter");
   quota_kernel<<<1, 1024, 0, st>>>(s->tab, s->slots, q, s->ppl, s->leaves);
-  // narrow steps: a warp per search, four per block; wide steps (>= 128 leaves
-  // per search): the whole block per search, 128 frontier entries per round
-  const bool wide = q >= kWideLeaves;
-  const uint32_t per_block = wide ? 1u : (uint32_t)(kSelectThreads / 32);
+  // narrow steps: a warp per search, four per block; wide steps (>= 128
+  // leaves per search): a block of 128-512 threads per search, as many
+  // frontier entries per round
+  const int team = select_team(q);
+  const uint32_t per_block = team == 32 ? (uint32_t)(kSelectThreads / 32) : 1u;
   const uint32_t sel_blocks = (s->slots + per_block - 1) / per_block;
+  const int threads = team == 32 ? kSelectThreads : team;
+  auto sel = [&](auto kernel) {
+    kernel<<<sel_blocks, threads, 0, st>>>(s->pool, s->tab, s->leaves, s->slots, s->ppl, s->lrn, s->ctl + 1);
+  };
   if (s->net) {
-    if (wide)
-      select_kernel<true, kSelectThreads><<<sel_blocks, kSelectThreads, 0, st>>>(s->pool, s->tab, s->leaves,
-                                                                               s->slots, s->ppl, s->lrn, s->ctl + 1);
-    else
-      select_kernel<true, 32><<<sel_blocks, kSelectThreads, 0, st>>>(s->pool, s->tab, s->leaves, s->slots, s->ppl,
-                                                                    s->lrn, s->ctl + 1);
+    switch (team) {
+      case 32: sel(select_kernel<true, 32>); break;
+      case 128: sel(select_kernel<true, 128>); break;
+      case 256: sel(select_kernel<true, 256>); break;
+      default: sel(select_kernel<true, 512>); break;
+    }
   } else {
-    if (wide)
-      select_kernel<false, kSelectThreads><<<sel_blocks, kSelectThreads, 0, st>>>(s->pool, s->tab, s->leaves,
-                                                                                s->slots, s->ppl, s->lrn, s->ctl + 1);
-    else
-      select_kernel<false, 32><<<sel_blocks, kSelectThreads, 0, st>>>(s->pool, s->tab, s->leaves, s->slots,
-                                                                     s->ppl, s->lrn, s->ctl + 1);
+    switch (team) {
+      case 32: sel(select_kernel<false, 32>); break;
+      case 128: sel(select_kernel<false, 128>); break;
+      case 256: sel(select_kernel<false, 256>); break;
+      default: sel(select_kernel<false, 512>); break;
+    }
   }
   PlayoutArgs a;
   a.pos = reinterpret_cast<const Board *>(s->leaves.board);

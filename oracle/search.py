@@ -12,8 +12,8 @@ every search's tree, so that a GPU test can compare the trees node for node:
              children share them equally, otherwise in proportion to UCB1
              weights rounded down, the rest one each to the heaviest children
              (first on ties).  The frontier is handled in chunks of 32 entries
-             (one warp's lanes; 128, the whole block, on steps of 128 leaves
-             per search or more); a chunk's expansions take node indices in
+             (one warp's lanes; on steps of 128 leaves per search or more a
+             block of 128, 256 or 512 threads); a chunk's expansions take node indices in
              entry order, and an expansion whose inclusive prefix of children
              would pass the search's node range plays out instead;
   playouts   slot i of a search's step uses random streams stream_next + i * ppl
@@ -56,7 +56,10 @@ MAX_CHILDREN = 64
 UNITS = 64
 PRIORS = 32
 TERMINAL_LEAF = F(2.0)
-WIDE_LEAVES, WIDE_TEAM = 128, 128  # steps of 128+ leaves per search: a 128-thread team per search
+def select_team(Q: int) -> int:
+    """Frontier entries per round of select_kernel for a step of Q leaves per
+    search: a warp (32) below 128, else a block of 128, 256 or 512 threads."""
+    return 32 if Q < 128 else (128 if Q < 256 else (256 if Q < 512 else 512))
 
 
 def _cf(bits: int) -> np.float32:
@@ -303,8 +306,7 @@ class SearchesOracle:
 
     def select(self, s: Search, q: int, team: int = 32):
         """select_kernel for one search: list of leaf node indices in emission
-        order.  `team`: frontier entries handled per round (32, a warp, or 128,
-        the block the kernel gives a search on steps of 128 leaves or more)."""
+        order.  `team`: frontier entries handled per round (select_team)."""
         learned = self.learned is not None
         leaves = []
         frontier = [(0, q)]
@@ -365,7 +367,7 @@ class SearchesOracle:
         playouts per leaf), when given, stands in for the replayed playouts
         (learned-proposal playouts, whose parity is checked on their own)."""
         qs = self.quota(Q)
-        team = WIDE_TEAM if Q >= WIDE_LEAVES else 32
+        team = select_team(Q)
         slots = []
         for si, (s, q) in enumerate(zip(self.slots, qs)):
             if s is None or q == 0:

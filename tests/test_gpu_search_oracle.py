@@ -96,13 +96,15 @@ def test_playouts_per_leaf_and_node_range_limits():
 
 
 def test_wide_steps_block_per_search():
-    """Steps of 128 and 512 leaves per search, where a whole block selects for
-    one search (128 frontier entries per round), with a node range that runs
-    out in the middle of a round."""
+    """Steps of 128, 256 and 512 leaves per search, where a whole block of as
+    many threads selects for one search (that many frontier entries per
+    round), with a node range that runs out in the middle of a round."""
     roots = list(L.random_positions(26, 3, 0, 30))
     _run(policy=0, ppl=2, q=128, budgets=[6000, 4000, 2000], caps=[150, 12000, 12000], roots=roots, graph=True,
          steps=30)
     _run(policy=0, ppl=1, q=512, budgets=[8000, 5000, 3000], caps=[700, 20000, 20000], roots=roots, graph=False,
+         steps=30)
+    _run(policy=2, ppl=2, q=256, budgets=[7000, 3000, 5000], caps=[20000, 400, 20000], roots=roots, graph=True,
          steps=30)
 
 
