@@ -117,9 +117,10 @@ __global__ void __launch_bounds__(BLOCK, (playout_min_blocks<POLICY, BLOCK>())) 
     // legal move (about two thirds) follow their chain at once; the others,
     // men's multi-jumps (about 1% of plies) and plies where a king's capture
     // can continue (about 0.2%, the costlier depth-first search), are deferred
-    // to every kMenPeriod-th and every king_period(POLICY)-th iteration, so
-    // that the lanes needing that code run it together and the other
-    // iterations stay branch-free.
+    // to every kMenPeriod-th (eps-greedy and reference heuristic only:
+    // defer_men) and every king_period(POLICY)-th iteration, so that the lanes
+    // needing that code run it together and the other iterations stay
+    // branch-free.
     // Once the work counter is exhausted, a warp with sparse_lanes(POLICY) or fewer
     // games defers nothing: its few games are latency-bound.
     //
@@ -269,7 +270,7 @@ __global__ void __launch_bounds__(BLOCK, (playout_min_blocks<POLICY, BLOCK>())) 
         }
         if (have) rs.refill();
       }
-      const bool men_ok = sparse || swapped || (it & (kMenPeriod - 1u)) == kMenPhase;
+      const bool men_ok = !defer_men(POLICY) || sparse || swapped || (it & (kMenPeriod - 1u)) == kMenPhase;
       const bool king_ok = sparse || swapped || (it & (king_period(POLICY) - 1u)) == kKingPhase;
       bool deferred_now = false;  // this iteration's ply was deferred (a candidate for the pending pool)
       do {
