@@ -29,6 +29,12 @@
 //   adam          sums the partials in a fixed order, updates the FP32 master
 //                 parameters, writes the BF16 copies W1..W3 and W2^T, W3^T
 // Every reduction has a fixed order, so a training run is reproducible.
+// The chain features .. F3, loss, B1, B3, B5 runs on the network's stream,
+// each kernel launched while the one before it drains (programmatic
+// dependent launch); B2 and its row sums run on a second stream, B4 and the
+// remaining row sums on a third.  dZ3 and dZ3^T are all zero between steps:
+// the loss writes at most 32 entries of a row and clear_dz3_kernel zeroes
+// them again once B1 and B2 have read them.
 #include "net.h"
 
 #include "launch.h"
@@ -41,7 +47,10 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <initializer_list>
 #include <mutex>
+#include <vector>
+#include <utility>
 #include <string>
 
 using bf16 = __nv_bfloat16;
@@ -49,11 +58,18 @@ using bf16 = __nv_bfloat16;
 struct gpuai_net {
   int device = 0;
   cudaStream_t stream = nullptr;
-  // the backward pass's second stream: the products and sums off the critical
-  // path (dW3, dW2, the bias gradients, the loss means) overlap the chain
-  // loss -> dZ2 -> dZ1 -> dW1 on `stream`
-  cudaStream_t side = nullptr;
-  cudaEvent_t ev_loss = nullptr, ev_b1 = nullptr, ev_b3 = nullptr, ev_side = nullptr;
+  // the backward pass's second and third streams: the products and sums off
+  // the critical path overlap the chain loss -> dZ2 -> dZ1 -> dW1 on
+  // `stream`; `side` takes dW3, db3, dwv, the loss means and dbv once the loss
+  // is known, `side2` dW2 and db2 once dZ2 is, and db1 once dZ1 is
+  cudaStream_t side = nullptr, side2 = nullptr;
+  cudaEvent_t ev_loss = nullptr, ev_b1 = nullptr, ev_b3 = nullptr, ev_side = nullptr, ev_side2 = nullptr,
+              ev_clear = nullptr;
+  // dZ3 and dZ3^T hold zeros between steps: the loss kernel writes at most 32
+  // entries per row and clear_dz3_kernel zeroes them again once both readers
+  // are done.  Set when a step stopped between the two (both are then cleared
+  // in full before the next step).
+  bool dz_dirty = false;
   uint32_t rows = 0;  // training batch capacity (multiple of 128)
   std::vector<void *> allocs;
   float *params = nullptr, *adam_m = nullptr, *adam_v = nullptr, *grad = nullptr;
@@ -76,12 +92,14 @@ struct gpuai_net {
   ga::Board *prop_cur = nullptr;
   size_t prop_cur_cap = 0;
   // the training step as one CUDA graph (for its batch size, tau and value
-  // coefficient): it reads the rows from the staging buffers and the learning
-  // rate and bias corrections from `hyper`
+  // coefficient), and its kernel nodes whose arguments change from step to
+  // step: the ones that read the rows, and Adam's (learning rate, bias
+  // corrections)
+  cudaGraph_t train_g = nullptr;
   cudaGraphExec_t train_graph = nullptr;
+  cudaGraphNode_t node_features = nullptr, node_loss = nullptr, node_clear = nullptr, node_adam = nullptr;
   uint32_t graph_n = 0;
   float graph_tau = 0.0f, graph_vcoef = 0.0f;
-  float *hyper = nullptr;
   std::mutex mu;
 };
 
@@ -131,12 +149,15 @@ struct GemmArgs {
   uint32_t skip_loads;  // self-test of the bounded waits: issue no TMA load, so the MMA warp's wait runs out
 };
 
-constexpr uint32_t kBM = 128, kBK = 64, kMaxStages = 4;
+constexpr uint32_t kBM = 128, kBK = 64, kMaxStages = 8;
 constexpr uint32_t kThreads = 256;            // 8 warps: two per TMEM lane quadrant in the epilogue
 constexpr uint32_t kABytes = kBM * kBK * 2;   // one A stage: 16 KiB
 constexpr uint32_t kSmemLimit = 227u * 1024u;
 constexpr uint32_t kRingBudget = 100u * 1024u;  // ring size that leaves room for two CTAs per SM
-constexpr uint32_t kSmemExtra = 1024u + 128u + 1024u;  // alignment slack, barriers, value-head partials
+constexpr uint32_t kBarBytes = 256u;  // full[] and empty[] (kMaxStages each), accf, TMEM slot, error flag
+constexpr uint32_t kSmemExtra = 1024u + kBarBytes + 1024u;  // alignment slack, barriers, value-head partials
+static_assert((2u * kMaxStages + 1u) * 8u + 8u <= kBarBytes, "barriers outgrow their slot");
+static_assert(2u * kRingBudget + kSmemExtra <= kSmemLimit, "doubled ring above the shared-memory limit");
 
 __device__ __forceinline__ uint32_t pack2(float a, float b) {
   __nv_bfloat162 h = __floats2bfloat162_rn(a, b);  // a in the low half
@@ -147,9 +168,9 @@ __device__ __forceinline__ float lo_bf(uint32_t w) { return __uint_as_float(w <<
 __device__ __forceinline__ float hi_bf(uint32_t w) { return __uint_as_float(w & 0xffff0000u); }
 __device__ __forceinline__ bool positive_bf(uint32_t h16) { return (h16 & 0x8000u) == 0 && (h16 & 0x7fffu) != 0; }
 
-// Epilogue of 32 consecutive columns col0.. of one row.
-__device__ __forceinline__ void epilogue32(const Epi &e, float (&v)[32], uint32_t row, uint32_t col0,
-                                           uint32_t split, float &vsum) {
+// Epilogue arithmetic on 32 consecutive columns col0.. of one row (lane's own
+// row): bias, rank-1 term, ReLU, ReLU mask.
+__device__ __forceinline__ void epilogue_math(const Epi &e, float (&v)[32], uint32_t row, uint32_t col0) {
   const uint32_t f = e.flags;
   if (f & kEpiBias) {  // column vectors are 16-byte aligned: col0 is a multiple of 32
     const float4 *bp = reinterpret_cast<const float4 *>(e.bias + col0);
@@ -191,29 +212,81 @@ __device__ __forceinline__ void epilogue32(const Epi &e, float (&v)[32], uint32_
       }
     }
   }
+}
+
+// Per-warp staging area of the epilogue stores (reuses the operand ring once
+// the MMAs are done): 32 rows x 36 floats, or 32 rows x 20 words of BF16
+// pairs, or 32 columns x 40 BF16 values of the transpose.  The padding keeps
+// each row 16-byte aligned and spreads a phase's accesses over the banks.
+constexpr uint32_t kStageF32 = 36, kStageB16 = 20, kStageB16T = 40;
+constexpr uint32_t kStageBytesPerWarp = 32u * kStageF32 * 4u;  // 4608
+constexpr uint32_t kStageBytes = 8u * kStageBytesPerWarp;      // eight warps
+
+// Stores of the 32 x 32 chunk at rows rbase.., columns col0.., whose values
+// lane l holds for row rbase + l.  The chunk goes through the warp's staging
+// area, so that a store instruction writes whole 32-byte sectors: 4 FP32
+// rows x 128 bytes, 8 BF16 rows x 64 bytes, or 8 columns x 64 bytes of the
+// BF16 transpose (instead of 16 bytes in each of 32 rows).  Rows >= `rows`
+// are not written.  Warp-collective.
+__device__ __forceinline__ void epilogue_store(const Epi &e, const float (&v)[32], uint8_t *stage, uint32_t rbase,
+                                               uint32_t rows, uint32_t lane, uint32_t col0, uint32_t split,
+                                               float &vsum) {
+  const uint32_t f = e.flags;
   if (f & (kEpiF32 | kEpiPartial)) {
-    float *o = e.out_f32 + ((f & kEpiPartial) ? (uint64_t)split * e.partial_stride : 0ull) +
-               (size_t)row * e.ld_f32 + col0;
+    float *st = reinterpret_cast<float *>(stage);
 #pragma unroll
     for (int q = 0; q < 8; q++)
-      reinterpret_cast<float4 *>(o)[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+      reinterpret_cast<float4 *>(st + lane * kStageF32)[q] =
+          make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+    __syncwarp();
+    float *o = e.out_f32 + ((f & kEpiPartial) ? (uint64_t)split * e.partial_stride : 0ull) + col0 + 4u * (lane & 7u);
+#pragma unroll
+    for (uint32_t k = 0; k < 8; k++) {
+      const uint32_t r = 4u * k + (lane >> 3);
+      const float4 t = reinterpret_cast<const float4 *>(st + r * kStageF32)[lane & 7u];
+      if (rbase + r < rows) *reinterpret_cast<float4 *>(o + (size_t)(rbase + r) * e.ld_f32) = t;
+    }
+    __syncwarp();
   }
   if (f & (kEpiB16 | kEpiB16T | kEpiVdot)) {
     uint32_t p[16];
 #pragma unroll
     for (int t = 0; t < 16; t++) p[t] = pack2(v[2 * t], v[2 * t + 1]);
     if (f & kEpiB16) {
-      uint4 *o = reinterpret_cast<uint4 *>(e.out_b + (size_t)row * e.ld_b + col0);
+      uint32_t *st = reinterpret_cast<uint32_t *>(stage);
 #pragma unroll
-      for (int q = 0; q < 4; q++) o[q] = make_uint4(p[4 * q], p[4 * q + 1], p[4 * q + 2], p[4 * q + 3]);
+      for (int q = 0; q < 4; q++)
+        reinterpret_cast<uint4 *>(st + lane * kStageB16)[q] = make_uint4(p[4 * q], p[4 * q + 1], p[4 * q + 2], p[4 * q + 3]);
+      __syncwarp();
+#pragma unroll
+      for (uint32_t k = 0; k < 4; k++) {
+        const uint32_t r = 8u * k + (lane >> 2), j = lane & 3u;
+        const uint4 t = reinterpret_cast<const uint4 *>(st + r * kStageB16)[j];
+        if (rbase + r < rows) reinterpret_cast<uint4 *>(e.out_b + (size_t)(rbase + r) * e.ld_b + col0)[j] = t;
+      }
+      __syncwarp();
     }
     if (f & kEpiB16T) {
-      uint16_t *o = reinterpret_cast<uint16_t *>(e.out_t) + (size_t)col0 * e.ld_t + row;
+      uint16_t *st = reinterpret_cast<uint16_t *>(stage);  // [column][row]
 #pragma unroll
       for (int t = 0; t < 16; t++) {
-        o[(size_t)(2 * t) * e.ld_t] = (uint16_t)(p[t] & 0xffffu);
-        o[(size_t)(2 * t + 1) * e.ld_t] = (uint16_t)(p[t] >> 16);
+        st[(2 * t) * kStageB16T + lane] = (uint16_t)(p[t] & 0xffffu);
+        st[(2 * t + 1) * kStageB16T + lane] = (uint16_t)(p[t] >> 16);
       }
+      __syncwarp();
+#pragma unroll
+      for (uint32_t k = 0; k < 4; k++) {
+        const uint32_t c = 8u * k + (lane >> 2), r0 = 8u * (lane & 3u);
+        const uint4 t = *reinterpret_cast<const uint4 *>(st + c * kStageB16T + r0);
+        uint16_t *o = reinterpret_cast<uint16_t *>(e.out_t) + (size_t)(col0 + c) * e.ld_t + rbase + r0;
+        if (rbase + r0 + 8u <= rows) {
+          *reinterpret_cast<uint4 *>(o) = t;
+        } else {
+          const uint32_t w[4] = {t.x, t.y, t.z, t.w};
+          for (uint32_t i = 0; i < 8u && rbase + r0 + i < rows; i++) o[i] = (uint16_t)(w[i >> 1] >> (16u * (i & 1u)));
+        }
+      }
+      __syncwarp();
     }
     if (f & kEpiVdot) {
       const float4 *wp = reinterpret_cast<const float4 *>(e.vdot_w + col0);
@@ -234,14 +307,18 @@ __global__ void __launch_bounds__(kThreads, 2)
   extern __shared__ uint8_t smem_raw[];
   uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023u) & ~(uintptr_t)1023u);
   const uint32_t bn = g.bn, stage_bytes = kABytes + bn * 128u, nst = g.stages;
-  uint64_t *full = reinterpret_cast<uint64_t *>(smem + nst * stage_bytes);
+  // [ring of nst stages, reused by the epilogue's staging][barriers][value-head partials]
+  const uint32_t area = nst * stage_bytes > kStageBytes ? nst * stage_bytes : kStageBytes;
+  uint64_t *full = reinterpret_cast<uint64_t *>(smem + area);
   uint64_t *empty = full + nst;
   uint64_t *accf = empty + nst;
   uint32_t *tslot = reinterpret_cast<uint32_t *>(accf + 1);
   uint32_t *s_err = tslot + 1;
-  float *vpart = reinterpret_cast<float *>(smem + nst * stage_bytes + 128u);  // [2][128] value-head partial sums
+  float *vpart = reinterpret_cast<float *>(smem + area + kBarBytes);  // [2][128] value-head partial sums
   const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
   const uint32_t row0 = blockIdx.x * kBM;
+  tc::grid_dep_wait();  // the operands come from the kernel before this one
+  tc::grid_dep_trigger();
   uint32_t rows = g.m_rows;
   if (g.dev_rows) {
     const uint32_t d = *g.dev_rows;
@@ -312,13 +389,18 @@ __global__ void __launch_bounds__(kThreads, 2)
   tc::fence_after_sync();
   const uint32_t quad = warp & 3u, half = warp >> 2;
   const uint32_t trow = quad * 32u + lane, row = row0 + trow;
-  const bool row_ok = row < rows && *s_err == 0;
+  // uniform over the warp: the staged stores below are warp-collective
+  const bool warp_ok = __all_sync(0xffffffffu, *s_err == 0u);
+  const bool row_ok = row < rows && warp_ok;
+  uint8_t *stage = smem + warp * kStageBytesPerWarp;  // the ring is free: every MMA has read its stage
   float vsum = 0.0f;
   const uint32_t c_lo = half * (bn / 2), c_hi = c_lo + bn / 2;
   for (uint32_t c = c_lo; c < c_hi; c += 32) {
     float v[32];
     tc::tmem_load32(tmem + ((quad * 32u) << 16) + c, v);  // warp-collective: every lane takes part
-    if (row_ok) epilogue32(g.e, v, row, blockIdx.y * bn + c, blockIdx.z, vsum);
+    const uint32_t col0 = blockIdx.y * bn + c;
+    if (row_ok) epilogue_math(g.e, v, row, col0);
+    if (warp_ok) epilogue_store(g.e, v, stage, row0 + quad * 32u, rows, lane, col0, blockIdx.z, vsum);
   }
   if (g.e.flags & kEpiVdot) vpart[half * kBM + trow] = vsum;
 
@@ -346,38 +428,84 @@ __device__ __forceinline__ uint32_t one_pair(uint32_t bits, int t) {
   return (((bits >> (2 * t)) & 1u) ? 0x3F80u : 0u) | (((bits >> (2 * t + 1)) & 1u) ? 0x3F800000u : 0u);
 }
 
-// X[r] = the 192 features of board r (zero rows past n); X^T optional.
+constexpr uint32_t kChunks = kInPad / 8;  // 8-feature chunks of a row of X
+constexpr uint32_t kXtChunks = 17;        // chunks holding a feature: 128 piece bits and the side to move
+
+// The four piece planes (own men, own kings, opponent men, opponent kings)
+// and the side to move of board r; all zero for r >= nn.
+__device__ __forceinline__ void board_planes(const gpuai_board *boards, uint32_t r, uint32_t nn, uint32_t (&pl)[4],
+                                             uint32_t &side) {
+  pl[0] = pl[1] = pl[2] = pl[3] = 0u;
+  side = 0u;
+  if (r >= nn) return;
+  const uint4 b = __ldg(reinterpret_cast<const uint4 *>(boards) + r);
+  side = b.w & 1u;
+  const uint32_t own = side ? b.y : b.x, opp = side ? b.x : b.y;
+  pl[0] = own & ~b.z;
+  pl[1] = own & b.z;
+  pl[2] = opp & ~b.z;
+  pl[3] = opp & b.z;
+}
+
+// X[r] = the 192 features of board r (zero rows past n), one 8-feature chunk
+// per thread (thread t: row t / 24, chunk t % 24).  With Xt, thread t also
+// writes features 8c .. 8c+7 of column r of X^T for c = t / rows, r = t % rows
+// (consecutive threads, consecutive columns); rows 136.. of X^T hold no
+// feature and stay zero from the network's creation.
 __global__ void features_kernel(const gpuai_board *boards, uint32_t n, const uint32_t *dev_n, uint32_t rows, bf16 *X,
                                 bf16 *Xt, uint32_t ldt) {
-  const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= rows) return;
+  tc::grid_dep_wait();
+  tc::grid_dep_trigger();
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
   uint32_t nn = n;
   if (dev_n) nn = *dev_n < rows ? *dev_n : rows;
-  uint32_t pl[4] = {0u, 0u, 0u, 0u}, side = 0;
-  if (r < nn) {
-    const uint4 b = __ldg(reinterpret_cast<const uint4 *>(boards) + r);
-    side = b.w & 1u;
-    const uint32_t own = side ? b.y : b.x, opp = side ? b.x : b.y;
-    pl[0] = own & ~b.z;
-    pl[1] = own & b.z;
-    pl[2] = opp & ~b.z;
-    pl[3] = opp & b.z;
-  }
-  uint4 *dst = reinterpret_cast<uint4 *>(X + (size_t)r * kInPad);
-#pragma unroll
-  for (uint32_t c = 0; c < kInPad / 8; c++) {
+  uint32_t pl[4], side;
+  if (t < rows * kChunks) {
+    const uint32_t r = t / kChunks, c = t - r * kChunks;
+    board_planes(boards, r, nn, pl, side);
     uint32_t bits = 0;
     if (c < 16) bits = (pl[c >> 2] >> ((c & 3u) * 8u)) & 0xffu;
     else if (c == 16) bits = side;
-    dst[c] = make_uint4(one_pair(bits, 0), one_pair(bits, 1), one_pair(bits, 2), one_pair(bits, 3));
+    reinterpret_cast<uint4 *>(X + (size_t)r * kInPad)[c] =
+        make_uint4(one_pair(bits, 0), one_pair(bits, 1), one_pair(bits, 2), one_pair(bits, 3));
   }
-  if (Xt) {
+  if (Xt && t < rows * kXtChunks) {
+    const uint32_t c = t / rows, r = t - c * rows;
+    board_planes(boards, r, nn, pl, side);
     uint16_t *xt = reinterpret_cast<uint16_t *>(Xt);
-    for (uint32_t f = 0; f < kInPad; f++) {
+#pragma unroll
+    for (uint32_t j = 0; j < 8; j++) {
+      const uint32_t f = 8u * c + j;
       const uint32_t bit = f < 128 ? (pl[f >> 5] >> (f & 31u)) & 1u : (f == 128 ? side : 0u);
       xt[(size_t)f * ldt + r] = bit ? 0x3F80u : 0u;
     }
   }
+}
+
+// The (from, to) pair of move `lane` of the list of board b (k moves,
+// 1 <= k <= 32), as from * 32 + to; lanes >= k get `none`.  Positions where no
+// capture can continue (nearly all) take each lane's move straight from the
+// move masks; the others walk the list.  Warp-collective: one board per warp.
+__device__ __forceinline__ uint32_t lane_pair(const Side &sd, uint32_t J, int &k, uint32_t lane, uint32_t none) {
+  uint32_t M[4];
+  bool capture;
+  if (simple_move_masks(sd, M, capture)) {
+    k = popc(M[0]) + popc(M[1]) + popc(M[2]) + popc(M[3]);
+    if (lane >= (uint32_t)k || k > (int)kMaxMoves) return none;
+    int from, to;
+    uint32_t removed;
+    nth_move(M[0], M[1], M[2], M[3], lane, capture, sd.own & ~sd.ownK, from, to, removed);
+    return (uint32_t)(from * 32 + to);
+  }
+  k = count_moves(sd, J);
+  if (k < 1 || k > (int)kMaxMoves) return none;
+  uint32_t pi = none, m = 0;
+  for_each_move(sd, J, [&](int from, int to, uint32_t, int, uint32_t) {
+    if (m == lane) pi = (uint32_t)(from * 32 + to);
+    m++;
+    return false;
+  });
+  return pi;
 }
 
 // One warp per row: value and policy loss terms and their gradients.  Lane m
@@ -386,6 +514,8 @@ __global__ void features_kernel(const gpuai_board *boards, uint32_t n, const uin
 __global__ void loss_kernel(const gpuai_board *boards, const float *z, const float *q, uint32_t n, uint32_t rows,
                             float tau, float vcoef, const float *logits, const float *vraw, bf16 *dZ3, bf16 *dZ3t,
                             uint32_t ldt, float *dv, float *rowloss) {
+  tc::grid_dep_wait();  // the logits and the value come from the kernel before this one
+  tc::grid_dep_trigger();
   const uint32_t r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31u;
   constexpr uint32_t kFull = 0xffffffffu;
   if (r >= rows) return;
@@ -408,16 +538,11 @@ __global__ void loss_kernel(const gpuai_board *boards, const float *z, const flo
   Side sd;
   make_side(b, sd);
   const uint32_t J = jumpers(sd);
-  const int k = count_moves(sd, J);
+  int k = 0;
+  // distinct placeholder for lanes without a move
+  const uint32_t pi = lane_pair(sd, J, k, lane, 0x10000u + lane);
   float ce = 0.0f;
   if (k >= 1 && k <= (int)kMaxMoves) {  // uniform over the warp
-    uint32_t pi = 0x10000u + lane;      // distinct placeholder for lanes without a move
-    uint32_t m = 0;
-    for_each_move(sd, J, [&](int from, int to, uint32_t, int, uint32_t) {
-      if (m == lane) pi = (uint32_t)(from * 32 + to);
-      m++;
-      return false;
-    });
     const bool act = lane < (uint32_t)k;
     const float qm = act ? q[(size_t)r * kMaxMoves + lane] : -3.0e38f;
     float qmax = qm;
@@ -428,10 +553,13 @@ __global__ void loss_kernel(const gpuai_board *boards, const float *z, const flo
     const float t = et / tsum;
     const uint32_t grp = __match_any_sync(kFull, pi);
     const bool leader = act && (uint32_t)(__ffs(grp) - 1) == lane;
-    float tp = 0.0f;  // target of this lane's pair: sum over the lanes sharing it, in lane order
-    for (int j = 0; j < 32; j++) {
-      const float tj = __shfl_sync(kFull, t, j);
-      if ((grp >> j) & 1u) tp += tj;
+    float tp = t;  // target of this lane's pair: sum over the lanes sharing it, in lane order
+    if (__any_sync(kFull, (grp & (grp - 1u)) != 0u)) {  // some pair has two moves (king captures)
+      tp = 0.0f;
+      for (int j = 0; j < 32; j++) {
+        const float tj = __shfl_sync(kFull, t, j);
+        if ((grp >> j) & 1u) tp += tj;
+      }
     }
     const float lg = leader ? logits[(size_t)r * kOut + pi] : -3.0e38f;
     float lmax = lg;
@@ -449,6 +577,23 @@ __global__ void loss_kernel(const gpuai_board *boards, const float *z, const flo
     for (int o = 16; o; o >>= 1) ce += __shfl_xor_sync(kFull, ce, o);
   }
   if (lane == 0) rowloss[2 * r] = ce;
+}
+
+// Zeroes the entries of dZ3 and dZ3^T that loss_kernel wrote for rows [0, n):
+// the (from, to) pairs of each row's legal moves, found the same way.
+__global__ void clear_dz3_kernel(const gpuai_board *boards, uint32_t n, bf16 *dZ3, bf16 *dZ3t, uint32_t ldt) {
+  const uint32_t r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31u;
+  if (r >= n) return;
+  const uint4 bv = __ldg(reinterpret_cast<const uint4 *>(boards) + r);
+  const Board b{bv.x, bv.y, bv.z, bv.w};
+  Side sd;
+  make_side(b, sd);
+  int k = 0;
+  const uint32_t pi = lane_pair(sd, jumpers(sd), k, lane, ~0u);
+  if (pi == ~0u) return;
+  const bf16 zero = __float2bfloat16_rn(0.0f);
+  dZ3[(size_t)r * kOut + pi] = zero;
+  dZ3t[(size_t)pi * ldt + r] = zero;
 }
 
 // out[row] = sum over the first ncols columns of M[row] (times vec[col] if
@@ -514,13 +659,28 @@ struct AdamArgs {
   const float *p1, *p2, *p3;
   uint32_t s1, s2, s3;    // split-K partial counts of dW1, dW2, dW3
   float lr, bc1, bc2;
-  const float *hyper;     // optional device {lr, bc1, bc2} (the graphed training step), else the fields above
   uint32_t mode;          // 0 update, 1 write the gradient to g_out, 2 refresh the BF16 copies only
   float *g_out;
   bf16 *W1b, *W2b, *W3b, *W2T, *W3T;
 };
 
 constexpr float kBeta1 = 0.9f, kBeta2 = 0.999f, kAdamEps = 1e-8f;
+
+// p[0] + p[stride] + ... + p[(count - 1) * stride], added in that order; the
+// loads are issued eight at a time.
+__device__ __forceinline__ float sum_partials(const float *p, size_t stride, uint32_t count) {
+  float g = 0.0f;
+  uint32_t s = 0;
+  for (; s + 8u <= count; s += 8u) {
+    float t[8];
+#pragma unroll
+    for (uint32_t j = 0; j < 8; j++) t[j] = __ldg(p + (size_t)(s + j) * stride);
+#pragma unroll
+    for (uint32_t j = 0; j < 8; j++) g += t[j];
+  }
+  for (; s < count; s++) g += __ldg(p + (size_t)s * stride);
+  return g;
+}
 
 __global__ void adam_kernel(AdamArgs a) {
   const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -529,11 +689,11 @@ __global__ void adam_kernel(AdamArgs a) {
   if (a.mode != 2) {
     float g = 0.0f;
     if (i < oB1) {
-      for (uint32_t s = 0; s < a.s1; s++) g += a.p1[(size_t)s * (kH * kInPad) + (i - oW1)];
+      g = sum_partials(a.p1 + (i - oW1), (size_t)kH * kInPad, a.s1);
     } else if (i >= oW2 && i < oB2) {
-      for (uint32_t s = 0; s < a.s2; s++) g += a.p2[(size_t)s * (kH * kH) + (i - oW2)];
+      g = sum_partials(a.p2 + (i - oW2), (size_t)kH * kH, a.s2);
     } else if (i >= oW3 && i < oB3) {
-      for (uint32_t s = 0; s < a.s3; s++) g += a.p3[(size_t)s * (kOut * kH) + (i - oW3)];
+      g = sum_partials(a.p3 + (i - oW3), (size_t)kOut * kH, a.s3);
     } else {
       g = a.g_direct[i];
     }
@@ -541,8 +701,7 @@ __global__ void adam_kernel(AdamArgs a) {
       a.g_out[i] = g;
       return;
     }
-    const float lr = a.hyper ? a.hyper[0] : a.lr, bc1 = a.hyper ? a.hyper[1] : a.bc1,
-                bc2 = a.hyper ? a.hyper[2] : a.bc2;
+    const float lr = a.lr, bc1 = a.bc1, bc2 = a.bc2;
     const float m = kBeta1 * a.m[i] + (1.0f - kBeta1) * g;
     const float v = kBeta2 * a.v[i] + (1.0f - kBeta2) * g * g;
     a.m[i] = m;
@@ -562,14 +721,6 @@ __global__ void adam_kernel(AdamArgs a) {
     a.W3b[j] = wb;
     a.W3T[c * kOut + r] = wb;
   }
-}
-
-// The step's learning rate and bias corrections into device memory, where the
-// graphed training step's Adam kernel reads them.
-__global__ void hyper_kernel(float *hyper, float lr, float bc1, float bc2) {
-  hyper[0] = lr;
-  hyper[1] = bc1;
-  hyper[2] = bc2;
 }
 
 __global__ void tanh_kernel(const float *x, uint32_t n, float *y) {
@@ -676,9 +827,40 @@ cudaError_t make_map(CUtensorMap *m, const void *base, uint64_t rows, uint64_t k
   return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
 }
 
+// Multiprocessors of the current device (read once).
+uint32_t sm_count() {
+  static uint32_t n = 0;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    int dev = 0, v = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess && cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) ==
+                                                  cudaSuccess)
+      n = (uint32_t)v;
+  });
+  return n;
+}
+
+// Launches `kernel`; with `pdl` it may start before the kernel ahead of it in
+// the stream has finished (the kernel then waits for it with grid_dep_wait).
+template <class... Params, class... Args>
+cudaError_t launch(void (*kernel)(Params...), dim3 grid, uint32_t threads, uint32_t smem, cudaStream_t s, bool pdl,
+                   Args &&...args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = dim3(threads);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = pdl ? 1u : 0u;
+  return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
+
 cudaError_t gemm(const CUtensorMap &a, const CUtensorMap &b, uint32_t m_rows, uint32_t n_total, uint32_t bn,
                  uint32_t kb_total, uint32_t splits, const uint32_t *dev_rows, uint32_t *status, const Epi &e,
-                 cudaStream_t s, uint64_t wait_ns = tc::kWaitLimitNs, bool skip_loads = false) {
+                 cudaStream_t s, bool pdl = false, uint64_t wait_ns = tc::kWaitLimitNs, bool skip_loads = false) {
   if (m_rows % kBM || bn % 64 || bn == 0 || bn > 256 || n_total % bn || splits == 0 || kb_total % splits)
     return cudaErrorInvalidValue;
   if ((e.flags & kEpiVdot) && n_total != bn) return cudaErrorInvalidValue;  // the value head needs whole rows
@@ -688,7 +870,13 @@ cudaError_t gemm(const CUtensorMap &a, const CUtensorMap &b, uint32_t m_rows, ui
   g.tmem_cols = bn <= 64 ? 64u : (bn <= 128 ? 128u : 256u);
   g.kb_per_split = kb_total / splits;
   const uint32_t stage_bytes = kABytes + bn * 128u;
-  uint32_t st = kRingBudget / stage_bytes;
+  // A product of the training step's critical chain (the launches with
+  // `pdl`) whose grid is at most one CTA per SM gets twice the ring: more
+  // loads in flight.  The side streams' products keep room for a second CTA
+  // on each SM, where they run beside the chain.
+  const uint32_t ctas = (m_rows / kBM) * (n_total / bn) * splits;
+  const uint32_t budget = pdl && ctas <= sm_count() ? 2u * kRingBudget : kRingBudget;
+  uint32_t st = budget / stage_bytes;
   st = st < 2 ? 2 : (st > kMaxStages ? kMaxStages : st);
   g.stages = g.kb_per_split < st ? g.kb_per_split : st;
   g.dev_rows = dev_rows;
@@ -696,10 +884,10 @@ cudaError_t gemm(const CUtensorMap &a, const CUtensorMap &b, uint32_t m_rows, ui
   g.e = e;
   g.wait_ns = wait_ns;
   g.skip_loads = skip_loads ? 1u : 0u;
-  const uint32_t smem = g.stages * stage_bytes + kSmemExtra;
+  const uint32_t ring = g.stages * stage_bytes;
+  const uint32_t smem = (ring > kStageBytes ? ring : kStageBytes) + kSmemExtra;
   if (smem > kSmemLimit) return cudaErrorInvalidValue;
-  gemm_kernel<<<dim3(m_rows / kBM, n_total / bn, splits), kThreads, smem, s>>>(a, b, g);
-  return cudaGetLastError();
+  return launch(gemm_kernel, dim3(m_rows / kBM, n_total / bn, splits), kThreads, smem, s, pdl, a, b, g);
 }
 
 uint32_t pick_splits(uint32_t kb, uint32_t target) {
@@ -749,7 +937,7 @@ namespace {
 cudaError_t forward_impl(const gpuai_net *net, Fwd &w, const gpuai_board *boards, uint32_t n, const uint32_t *dev_n,
                          uint32_t rows, uint32_t *status, bool train, cudaStream_t s) {
   const float *P = net->params;
-  features_kernel<<<(rows + 127) / 128, 128, 0, s>>>(boards, n, dev_n, rows, w.X, train ? net->Xt : nullptr,
+  features_kernel<<<(rows * kChunks + 255) / 256, 256, 0, s>>>(boards, n, dev_n, rows, w.X, train ? net->Xt : nullptr,
                                                      net->rows);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
@@ -760,7 +948,8 @@ cudaError_t forward_impl(const gpuai_net *net, Fwd &w, const gpuai_board *boards
   e1.ld_b = kH;
   e1.out_t = net->H1t;
   e1.ld_t = net->rows;
-  if ((e = gemm(w.mX, net->mW1, rows, kH, kBnF1, kInPad / kBK, 1, dev_n, status, e1, s)) != cudaSuccess) return e;
+  if ((e = gemm(w.mX, net->mW1, rows, kH, kBnF1, kInPad / kBK, 1, dev_n, status, e1, s, train)) != cudaSuccess)
+    return e;
   Epi e2 = e1;
   e2.flags |= kEpiVdot;
   e2.bias = P + oB2;
@@ -769,7 +958,8 @@ cudaError_t forward_impl(const gpuai_net *net, Fwd &w, const gpuai_board *boards
   e2.vdot_w = P + oWV;
   e2.vdot_b = P + oBV;
   e2.vdot_out = w.vraw;
-  if ((e = gemm(w.mH1, net->mW2, rows, kH, kBnF2, kH / kBK, 1, dev_n, status, e2, s)) != cudaSuccess) return e;
+  if ((e = gemm(w.mH1, net->mW2, rows, kH, kBnF2, kH / kBK, 1, dev_n, status, e2, s, train)) != cudaSuccess)
+    return e;
   Epi e3;
   e3.flags = kEpiBias | (w.logits_b ? kEpiB16 : kEpiF32);
   e3.bias = P + oB3;
@@ -777,7 +967,7 @@ cudaError_t forward_impl(const gpuai_net *net, Fwd &w, const gpuai_board *boards
   e3.ld_f32 = kOut;
   e3.out_b = w.logits_b;
   e3.ld_b = kOut;
-  return gemm(w.mH2, net->mW3, rows, kOut, kBnF3, kH / kBK, 1, dev_n, status, e3, s);
+  return gemm(w.mH2, net->mW3, rows, kOut, kBnF3, kH / kBK, 1, dev_n, status, e3, s, train);
 }
 
 // Forward + backward on rows [0, n) of the training workspace; gradients are
@@ -788,18 +978,18 @@ cudaError_t backward_impl(gpuai_net *net, const gpuai_board *boards, const float
   const float *P = net->params;
   cudaError_t e = forward_impl(net, net->fw, boards, n, nullptr, B, net->status, true, s);
   if (e != cudaSuccess) return e;
-  if ((e = cudaMemsetAsync(net->dZ3, 0, (size_t)B * kOut * sizeof(bf16), s)) != cudaSuccess) return e;
-  if ((e = cudaMemset2DAsync(net->dZ3t, (size_t)L * sizeof(bf16), 0, (size_t)B * sizeof(bf16), kOut, s)) !=
-      cudaSuccess)
+  // The chain forward -> loss -> dZ2 -> dZ1 -> dW1 launches each kernel while
+  // the one before it drains (programmatic dependent launch); dZ3 and dZ3^T
+  // are zero on entry apart from what this step's loss kernel writes.
+  net->dz_dirty = true;  // until clear_dz3_kernel is queued
+  if ((e = launch(loss_kernel, dim3(B / 4), 128, 0, s, true, boards, z, q, n, B, tau, vcoef, net->fw.logits,
+                  net->fw.vraw, net->dZ3, net->dZ3t, L, net->dv, net->rowloss)) != cudaSuccess)
     return e;
-  loss_kernel<<<B / 4, 128, 0, s>>>(boards, z, q, n, B, tau, vcoef, net->fw.logits, net->fw.vraw, net->dZ3,
-                                      net->dZ3t, L, net->dv, net->rowloss);
-  if ((e = cudaGetLastError()) != cudaSuccess) return e;
   const uint32_t kb = B / kBK;
   splits[2] = pick_splits(kb, kSplit3);
   splits[1] = pick_splits(kb, kSplit2);
   splits[0] = pick_splits(kb, kSplit1);
-  const cudaStream_t t = net->side;
+  const cudaStream_t t = net->side, u = net->side2;
   // side stream, after the loss: dW3 partials, db3, dwv, the loss means and dbv
   if ((e = cudaEventRecord(net->ev_loss, s)) != cudaSuccess) return e;
   if ((e = cudaStreamWaitEvent(t, net->ev_loss, 0)) != cudaSuccess) return e;
@@ -814,6 +1004,7 @@ cudaError_t backward_impl(gpuai_net *net, const gpuai_board *boards, const float
   rowsum_kernel<<<kH, 256, 0, t>>>(net->H2t, B, L, net->dv, net->grad + oWV);
   loss_reduce_kernel<<<1, 256, 0, t>>>(net->rowloss, net->dv, n, B, net->loss2, net->grad + oBV);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  if ((e = cudaEventRecord(net->ev_side, t)) != cudaSuccess) return e;
   Epi b1;
   b1.flags = kEpiRank1 | kEpiMask | kEpiB16 | kEpiB16T;
   b1.r1_row = net->dv;
@@ -824,19 +1015,27 @@ cudaError_t backward_impl(gpuai_net *net, const gpuai_board *boards, const float
   b1.ld_b = kH;
   b1.out_t = net->dZ2t;
   b1.ld_t = L;
-  if ((e = gemm(net->mdZ3, net->mW3T, B, kH, kBnB1, kOut / kBK, 1, nullptr, net->status, b1, s)) != cudaSuccess)
+  if ((e = gemm(net->mdZ3, net->mW3T, B, kH, kBnB1, kOut / kBK, 1, nullptr, net->status, b1, s, true)) !=
+      cudaSuccess)
     return e;
-  // side stream, after dZ2: dW2 partials and db2
+  // third stream, after dZ2: dW2 partials and db2; side stream: dZ3 (read
+  // by dZ2's product) and dZ3^T (dW3's) back to zero, which nothing in the
+  // step waits for (the main stream joins it at the end of the step)
   if ((e = cudaEventRecord(net->ev_b1, s)) != cudaSuccess) return e;
+  if ((e = cudaStreamWaitEvent(u, net->ev_b1, 0)) != cudaSuccess) return e;
   if ((e = cudaStreamWaitEvent(t, net->ev_b1, 0)) != cudaSuccess) return e;
+  clear_dz3_kernel<<<B / 4, 128, 0, t>>>(boards, n, net->dZ3, net->dZ3t, L);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  if ((e = cudaEventRecord(net->ev_clear, t)) != cudaSuccess) return e;
+  net->dz_dirty = false;
   Epi b4;
   b4.flags = kEpiPartial;
   b4.out_f32 = net->p2;
   b4.ld_f32 = kH;
   b4.partial_stride = (uint64_t)kH * kH;
-  if ((e = gemm(net->mdZ2t, net->mH1t, kH, kH, kBnB4, kb, splits[1], nullptr, net->status, b4, t)) != cudaSuccess)
+  if ((e = gemm(net->mdZ2t, net->mH1t, kH, kH, kBnB4, kb, splits[1], nullptr, net->status, b4, u)) != cudaSuccess)
     return e;
-  rowsum_kernel<<<kH, 256, 0, t>>>(net->dZ2t, B, L, nullptr, net->grad + oB2);
+  rowsum_kernel<<<kH, 256, 0, u>>>(net->dZ2t, B, L, nullptr, net->grad + oB2);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   Epi b3;
   b3.flags = kEpiMask | kEpiB16T;
@@ -844,29 +1043,42 @@ cudaError_t backward_impl(gpuai_net *net, const gpuai_board *boards, const float
   b3.ld_mask = kH;
   b3.out_t = net->dZ1t;
   b3.ld_t = L;
-  if ((e = gemm(net->mdZ2, net->mW2T, B, kH, kBnB3, kH / kBK, 1, nullptr, net->status, b3, s)) != cudaSuccess)
+  if ((e = gemm(net->mdZ2, net->mW2T, B, kH, kBnB3, kH / kBK, 1, nullptr, net->status, b3, s, true)) !=
+      cudaSuccess)
     return e;
-  // side stream, after dZ1: db1; then the main stream waits for the side's work
+  // third stream, after dZ1: db1; then the main stream waits for both side streams
   if ((e = cudaEventRecord(net->ev_b3, s)) != cudaSuccess) return e;
-  if ((e = cudaStreamWaitEvent(t, net->ev_b3, 0)) != cudaSuccess) return e;
-  rowsum_kernel<<<kH, 256, 0, t>>>(net->dZ1t, B, L, nullptr, net->grad + oB1);
+  if ((e = cudaStreamWaitEvent(u, net->ev_b3, 0)) != cudaSuccess) return e;
+  rowsum_kernel<<<kH, 256, 0, u>>>(net->dZ1t, B, L, nullptr, net->grad + oB1);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
-  if ((e = cudaEventRecord(net->ev_side, t)) != cudaSuccess) return e;
+  if ((e = cudaEventRecord(net->ev_side2, u)) != cudaSuccess) return e;
   Epi b5;
   b5.flags = kEpiPartial;
   b5.out_f32 = net->p1;
   b5.ld_f32 = kInPad;
   b5.partial_stride = (uint64_t)kH * kInPad;
-  if ((e = gemm(net->mdZ1t, net->mXt, kH, kInPad, kBnB5, kb, splits[0], nullptr, net->status, b5, s)) !=
+  if ((e = gemm(net->mdZ1t, net->mXt, kH, kInPad, kBnB5, kb, splits[0], nullptr, net->status, b5, s, true)) !=
       cudaSuccess)
     return e;
-  return cudaStreamWaitEvent(s, net->ev_side, 0);
+  if ((e = cudaStreamWaitEvent(s, net->ev_side, 0)) != cudaSuccess) return e;
+  return cudaStreamWaitEvent(s, net->ev_side2, 0);
 }
 
-cudaError_t run_adam(gpuai_net *net, uint32_t mode, const uint32_t *splits, float lr, cudaStream_t s,
-                     const float *hyper = nullptr) {
+// Joins the side stream's clearing of dZ3 / dZ3^T into `s` (after the
+// step's last kernel on `s`, so nothing there waits for it).
+cudaError_t join_clear(gpuai_net *net, cudaStream_t s) { return cudaStreamWaitEvent(s, net->ev_clear, 0); }
+
+// dZ3 and dZ3^T in full back to zero after a step that stopped half-way.
+cudaError_t clear_dz3_full(gpuai_net *net, cudaStream_t s) {
+  if (!net->dz_dirty) return cudaSuccess;
+  cudaError_t e = cudaMemsetAsync(net->dZ3, 0, (size_t)net->rows * kOut * sizeof(bf16), s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(net->dZ3t, 0, (size_t)kOut * net->rows * sizeof(bf16), s);
+  if (e == cudaSuccess) net->dz_dirty = false;
+  return e;
+}
+
+cudaError_t run_adam(gpuai_net *net, uint32_t mode, const uint32_t *splits, float lr, cudaStream_t s) {
   AdamArgs a;
-  a.hyper = hyper;
   a.w = net->params;
   a.m = net->adam_m;
   a.v = net->adam_v;
@@ -889,6 +1101,50 @@ cudaError_t run_adam(gpuai_net *net, uint32_t mode, const uint32_t *splits, floa
   a.W3T = net->W3T;
   adam_kernel<<<(uint32_t)((kParams + 255) / 256), 256, 0, s>>>(a);
   return cudaGetLastError();
+}
+
+template <class... P>
+constexpr uint32_t nparams(void (*)(P...)) {
+  return (uint32_t)sizeof...(P);
+}
+
+// The one kernel node of graph g that runs `func`.
+cudaError_t find_kernel_node(cudaGraph_t g, const void *func, cudaGraphNode_t *out) {
+  size_t count = 0;
+  cudaError_t e = cudaGraphGetNodes(g, nullptr, &count);
+  std::vector<cudaGraphNode_t> nodes(count);
+  if (e == cudaSuccess && count) e = cudaGraphGetNodes(g, nodes.data(), &count);
+  if (e != cudaSuccess) return e;
+  *out = nullptr;
+  for (cudaGraphNode_t node : nodes) {
+    cudaGraphNodeType t;
+    cudaKernelNodeParams p;
+    if (cudaGraphNodeGetType(node, &t) != cudaSuccess || t != cudaGraphNodeTypeKernel) continue;
+    if ((e = cudaGraphKernelNodeGetParams(node, &p)) != cudaSuccess) return e;
+    if (p.func != func) continue;
+    if (*out) return cudaErrorInvalidValue;  // more than one
+    *out = node;
+  }
+  return *out ? cudaSuccess : cudaErrorInvalidValue;
+}
+
+// Replaces arguments of kernel node `node` (nargs in all) of the instantiated
+// graph x: argument r.first by *r.second; the others keep their captured
+// values.  The next launch of x uses them.
+cudaError_t set_node_args(cudaGraphExec_t x, cudaGraphNode_t node, uint32_t nargs,
+                          std::initializer_list<std::pair<uint32_t, void *>> repl) {
+  cudaKernelNodeParams p;
+  cudaError_t e = cudaGraphKernelNodeGetParams(node, &p);
+  if (e != cudaSuccess) return e;
+  if (!p.kernelParams || p.extra || nargs > 16) return cudaErrorNotSupported;
+  void *args[16];
+  for (uint32_t i = 0; i < nargs; i++) args[i] = p.kernelParams[i];
+  for (const auto &r : repl) {
+    if (r.first >= nargs) return cudaErrorInvalidValue;
+    args[r.first] = r.second;
+  }
+  p.kernelParams = args;
+  return cudaGraphExecKernelNodeSetParams(x, node, &p);
 }
 
 int err(int code, const std::string &m) { return ga::record_error(code, m.c_str()); }
@@ -982,7 +1238,8 @@ int gpuai_net_create(int device, uint32_t max_batch, uint64_t init_seed, gpuai_n
   auto &A = net->allocs;
   cudaError_t e = cudaStreamCreateWithFlags(&net->stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&net->side, cudaStreamNonBlocking);
-  for (cudaEvent_t *ev : {&net->ev_loss, &net->ev_b1, &net->ev_b3, &net->ev_side})
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&net->side2, cudaStreamNonBlocking);
+  for (cudaEvent_t *ev : {&net->ev_loss, &net->ev_b1, &net->ev_b3, &net->ev_side, &net->ev_side2, &net->ev_clear})
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
   if (e == cudaSuccess) e = dalloc(A, &net->params, kParams);
   if (e == cudaSuccess) e = dalloc(A, &net->adam_m, kParams);
@@ -1014,7 +1271,6 @@ int gpuai_net_create(int device, uint32_t max_batch, uint64_t init_seed, gpuai_n
   if (e == cudaSuccess) e = dalloc(A, &net->in_boards, L);
   if (e == cudaSuccess) e = dalloc(A, &net->in_z, L);
   if (e == cudaSuccess) e = dalloc(A, &net->in_q, (size_t)L * kMaxMoves);
-  if (e == cudaSuccess) e = dalloc(A, &net->hyper, 4);
   if (e != cudaSuccess) return fail(cuda_err(e, "gpuai_net_create: allocation"));
   e = make_map(&net->mW1, net->W1b, kH, kInPad, kBnF1);
   if (e == cudaSuccess) e = make_map(&net->mW2, net->W2b, kH, kH, kBnF2);
@@ -1035,6 +1291,8 @@ int gpuai_net_create(int device, uint32_t max_batch, uint64_t init_seed, gpuai_n
   if (e == cudaSuccess) e = cudaMemsetAsync(net->Xt, 0, (size_t)kInPad * L * sizeof(bf16), net->stream);
   if (e == cudaSuccess) e = cudaMemsetAsync(net->H1t, 0, (size_t)kH * L * sizeof(bf16), net->stream);
   if (e == cudaSuccess) e = cudaMemsetAsync(net->H2t, 0, (size_t)kH * L * sizeof(bf16), net->stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(net->dZ3, 0, (size_t)L * kOut * sizeof(bf16), net->stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(net->dZ3t, 0, (size_t)kOut * L * sizeof(bf16), net->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(net->stream);
   if (e != cudaSuccess) return fail(cuda_err(e, "gpuai_net_create: clear"));
   std::vector<float> p;
@@ -1050,13 +1308,16 @@ void gpuai_net_destroy(gpuai_net *net) {
   cudaSetDevice(net->device);
   if (net->stream) cudaStreamSynchronize(net->stream);
   if (net->side) cudaStreamSynchronize(net->side);
+  if (net->side2) cudaStreamSynchronize(net->side2);
   if (net->train_graph) cudaGraphExecDestroy(net->train_graph);
+  if (net->train_g) cudaGraphDestroy(net->train_g);
   for (void *p : net->prop_allocs) cudaFree(p);
   if (net->prop_cur) cudaFree(net->prop_cur);
   for (void *p : net->allocs) cudaFree(p);
-  for (cudaEvent_t ev : {net->ev_loss, net->ev_b1, net->ev_b3, net->ev_side})
+  for (cudaEvent_t ev : {net->ev_loss, net->ev_b1, net->ev_b3, net->ev_side, net->ev_side2, net->ev_clear})
     if (ev) cudaEventDestroy(ev);
   if (net->side) cudaStreamDestroy(net->side);
+  if (net->side2) cudaStreamDestroy(net->side2);
   if (net->stream) cudaStreamDestroy(net->stream);
   delete net;
 }
@@ -1171,8 +1432,10 @@ int gpuai_net_gradients(gpuai_net *net, const gpuai_board *boards, const float *
   NCK(cudaMemcpyAsync(net->in_z, value_target, n * sizeof(float), cudaMemcpyHostToDevice, s), "H2D");
   NCK(cudaMemcpyAsync(net->in_q, move_q, (size_t)n * kMaxMoves * sizeof(float), cudaMemcpyHostToDevice, s), "H2D");
   uint32_t splits[3];
+  NCK(clear_dz3_full(net, s), "clear");
   NCK(backward_impl(net, net->in_boards, net->in_z, net->in_q, n, tau, value_coef, splits, s), "backward");
   NCK(run_adam(net, 1, splits, 0.0f, s), "gradient gather");
+  NCK(join_clear(net, s), "join");
   NCK(cudaMemcpyAsync(grads, net->gout, kParams * sizeof(float), cudaMemcpyDeviceToHost, s), "D2H");
   if (loss2) NCK(cudaMemcpyAsync(loss2, net->loss2, 2 * sizeof(float), cudaMemcpyDeviceToHost, s), "D2H");
   return check_status(net);
@@ -1184,40 +1447,62 @@ int gpuai_net_train_step(gpuai_net *net, const gpuai_board *d_boards, const floa
   if (!net || !d_boards || !d_value_target || !d_move_q) return err(GPUAI_ERR_INVALID, "gpuai_net_train_step: NULL");
   if (n == 0 || n > net->rows) return err(GPUAI_ERR_INVALID, "gpuai_net_train_step: n outside 1..max_batch");
   if (!(tau > 0.0f) || !(lr >= 0.0f)) return err(GPUAI_ERR_INVALID, "gpuai_net_train_step: bad tau or lr");
+  if (reinterpret_cast<uintptr_t>(d_boards) % 16 || reinterpret_cast<uintptr_t>(d_value_target) % 4 ||
+      reinterpret_cast<uintptr_t>(d_move_q) % 4)
+    return err(GPUAI_ERR_INVALID, "gpuai_net_train_step: rows not aligned (boards 16 bytes, values 4)");
   std::lock_guard<std::mutex> lock(net->mu);
   NCK(cudaSetDevice(net->device), "cudaSetDevice");
   const cudaStream_t s = net->stream;
-  // The step's ~25 launches are replayed as one CUDA graph: the rows are
-  // staged into the network's own buffers (fixed addresses for the graph),
-  // the learning rate and bias corrections go to device memory, and the
-  // graph is captured again only when the batch size, tau or the value
-  // coefficient change.  Same kernels in the same order: same results.
-  NCK(cudaMemcpyAsync(net->in_boards, d_boards, (size_t)n * sizeof(gpuai_board), cudaMemcpyDeviceToDevice, s),
-      "stage boards");
-  NCK(cudaMemcpyAsync(net->in_z, d_value_target, (size_t)n * sizeof(float), cudaMemcpyDeviceToDevice, s),
-      "stage values");
-  NCK(cudaMemcpyAsync(net->in_q, d_move_q, (size_t)n * kMaxMoves * sizeof(float), cudaMemcpyDeviceToDevice, s),
-      "stage move values");
+  // The step's ~25 launches are replayed as one CUDA graph, captured again
+  // only when the batch size, tau or the value coefficient change.  Before
+  // each replay the graph's kernels that read the rows (features, loss, the
+  // clearing of dZ3) get this step's row pointers, and Adam this step's
+  // learning rate and bias corrections, as new arguments of their nodes in the
+  // instantiated graph: no copy and no launch besides the graph itself.  Same
+  // kernels in the same order: same results.
+  NCK(clear_dz3_full(net, s), "clear");
   net->step++;
-  hyper_kernel<<<1, 1, 0, s>>>(net->hyper, lr, (float)(1.0 - std::pow(0.9, (double)net->step)),
-                               (float)(1.0 - std::pow(0.999, (double)net->step)));
-  NCK(cudaGetLastError(), "hyper");
   if (!net->train_graph || net->graph_n != n || net->graph_tau != tau || net->graph_vcoef != value_coef) {
     if (net->train_graph) cudaGraphExecDestroy(net->train_graph);
+    if (net->train_g) cudaGraphDestroy(net->train_g);
     net->train_graph = nullptr;
+    net->train_g = nullptr;
     cudaGraph_t g = nullptr;
     uint32_t splits[3];
     NCK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "begin capture");
-    cudaError_t e = backward_impl(net, net->in_boards, net->in_z, net->in_q, n, tau, value_coef, splits, s);
-    if (e == cudaSuccess) e = run_adam(net, 0, splits, 0.0f, s, net->hyper);
+    cudaError_t e = backward_impl(net, d_boards, d_value_target, d_move_q, n, tau, value_coef, splits, s);
+    if (e == cudaSuccess) e = run_adam(net, 0, splits, lr, s);
+    if (e == cudaSuccess) e = join_clear(net, s);
+    // nothing ran during the capture: dZ3 / dZ3^T are as the last replay left them
+    net->dz_dirty = false;
     const cudaError_t ec = cudaStreamEndCapture(s, &g);
     if (e == cudaSuccess) e = ec;
+    if (e == cudaSuccess) e = find_kernel_node(g, (const void *)features_kernel, &net->node_features);
+    if (e == cudaSuccess) e = find_kernel_node(g, (const void *)loss_kernel, &net->node_loss);
+    if (e == cudaSuccess) e = find_kernel_node(g, (const void *)clear_dz3_kernel, &net->node_clear);
+    if (e == cudaSuccess) e = find_kernel_node(g, (const void *)adam_kernel, &net->node_adam);
     if (e == cudaSuccess) e = cudaGraphInstantiate(&net->train_graph, g, 0);
-    if (g) cudaGraphDestroy(g);
+    if (e != cudaSuccess && g) cudaGraphDestroy(g);
     NCK(e, "training step graph");
+    net->train_g = g;
     net->graph_n = n;
     net->graph_tau = tau;
     net->graph_vcoef = value_coef;
+  }
+  {
+    cudaKernelNodeParams p;
+    NCK(cudaGraphKernelNodeGetParams(net->node_adam, &p), "graph update");
+    AdamArgs a = *static_cast<const AdamArgs *>(p.kernelParams[0]);
+    a.lr = lr;
+    a.bc1 = (float)(1.0 - std::pow(0.9, (double)net->step));
+    a.bc2 = (float)(1.0 - std::pow(0.999, (double)net->step));
+    const cudaGraphExec_t x = net->train_graph;
+    NCK(set_node_args(x, net->node_features, nparams(features_kernel), {{0u, &d_boards}}), "graph update");
+    NCK(set_node_args(x, net->node_loss, nparams(loss_kernel),
+                      {{0u, &d_boards}, {1u, &d_value_target}, {2u, &d_move_q}}),
+        "graph update");
+    NCK(set_node_args(x, net->node_clear, nparams(clear_dz3_kernel), {{0u, &d_boards}}), "graph update");
+    NCK(set_node_args(x, net->node_adam, nparams(adam_kernel), {{0u, &a}}), "graph update");
   }
   NCK(cudaGraphLaunch(net->train_graph, s), "training step");
   if (loss2) {
@@ -1241,7 +1526,7 @@ int gpuai_net_wait_selftest(gpuai_net *net, uint32_t wait_limit_us, uint32_t *st
   e1.bias = net->params + oB1;
   e1.out_b = net->fw.H1;
   e1.ld_b = kH;
-  NCK(gemm(net->fw.mX, net->mW1, kBM, kH, kBnF1, kInPad / kBK, 1, nullptr, net->status, e1, s,
+  NCK(gemm(net->fw.mX, net->mW1, kBM, kH, kBnF1, kInPad / kBK, 1, nullptr, net->status, e1, s, false,
            (uint64_t)wait_limit_us * 1000u, true),
       "self-test launch");
   uint32_t st = 0;

@@ -481,6 +481,38 @@ GA_HD void nth_move(uint32_t M0, uint32_t M1, uint32_t M2, uint32_t M3, uint32_t
   removed = capture ? 1u << mid : 0u;
 }
 
+// Move masks of a position in which no capture can continue, so that every
+// legal move is a direct move or a single jump: M[d] = the squares that move
+// in direction d and `capture` whether they jump; move i of the list is then
+// nth_move(M[0], M[1], M[2], M[3], i, capture, men, ...) and the count is
+// the masks' population.  Returns false when some capture can continue (the
+// list then needs the search, for_each_move).
+GA_HD bool simple_move_masks(const Side &s, uint32_t M[4], bool &capture) {
+  const uint32_t men = s.own & ~s.ownK;
+  const uint32_t m01 = s.turn ? s.ownK : s.own;  // D0/D1 movers: P1 men and all kings
+  const uint32_t m23 = s.turn ? s.own : s.ownK;  // D2/D3 movers: P2 men and all kings
+  const uint32_t J0 = m01 & s.jd[0], J1 = m01 & s.jd[1], J2 = m23 & s.jd[2], J3 = m23 & s.jd[3];
+  capture = (J0 | J1 | J2 | J3) != 0;
+  if (capture) {
+    const uint32_t jall = s.jd[0] | s.jd[1] | s.jd[2] | s.jd[3];
+    const uint32_t jf = s.turn ? (s.jd[2] | s.jd[3]) : (s.jd[0] | s.jd[1]);
+    const uint32_t lm = jump2<0>(J0 & men) | jump2<1>(J1 & men) | jump2<2>(J2 & men) | jump2<3>(J3 & men);
+    const uint32_t lk = jump2<0>(J0 & s.ownK) | jump2<1>(J1 & s.ownK) | jump2<2>(J2 & s.ownK) |
+                        jump2<3>(J3 & s.ownK);
+    if ((lk & jall) | (lm & jf)) return false;
+    M[0] = J0;
+    M[1] = J1;
+    M[2] = J2;
+    M[3] = J3;
+    return true;
+  }
+  M[0] = m01 & step<3>(s.empty);
+  M[1] = m01 & step<2>(s.empty);
+  M[2] = m23 & step<1>(s.empty);
+  M[3] = m23 & step<0>(s.empty);
+  return true;
+}
+
 // Squares of the side to move whose capture can continue after the first
 // jump (they need the depth-first search); J[d] are the first-jump sources.
 GA_HD uint32_t continuing_sources(const Side &s, const uint32_t J[4]) {

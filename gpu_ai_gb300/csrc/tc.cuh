@@ -25,6 +25,17 @@ __device__ __forceinline__ uint64_t globaltimer() {
   return t;
 }
 
+// ---- programmatic dependent launch
+
+// A kernel launched with the programmatic stream serialization attribute may
+// start while the kernel before it in the stream is still running.  It calls
+// grid_dep_wait() before its first global-memory access: that returns once
+// the kernel before it has completed and its writes are visible (at once for a
+// launch without the attribute).  grid_dep_trigger() lets the next such
+// kernel in the stream launch before this one has finished.
+__device__ __forceinline__ void grid_dep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void grid_dep_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 // ---- mbarriers
 
 __device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {

@@ -251,8 +251,11 @@ int gpuai_net_gradients(gpuai_net *net, const gpuai_board *boards, const float *
                         float *loss2);
 /* One Adam step (beta1 0.9, beta2 0.999, eps 1e-8) on device-resident
  * training rows d_boards[n], d_value_target[n], d_move_q[n*32], enqueued on the
- * net's stream.  loss2 (host, optional) makes the call wait and return the
- * step's mean policy and value losses. */
+ * net's stream.  The step's kernels read the rows in place: leave them
+ * unchanged until the net's stream has run the step; d_boards must be 16-byte
+ * aligned, the others 4-byte (GPUAI_ERR_INVALID otherwise).  loss2 (host,
+ * optional) makes the call wait and return the step's mean policy and value
+ * losses. */
 int gpuai_net_train_step(gpuai_net *net, const gpuai_board *d_boards, const float *d_value_target,
                          const float *d_move_q, uint32_t n, float lr, float tau, float value_coef, float *loss2);
 /* Training labels from GPU playouts, on device buffers: for each position,

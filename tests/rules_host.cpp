@@ -265,3 +265,52 @@ long rh_heur_fast_matches_enum(uint64_t n, uint64_t seed) {
   return bad;
 }
 }
+
+extern "C" {
+// simple_move_masks + nth_move (the network kernels' per-lane move list)
+// against for_each_move on n pseudo-random boards: on every board where no
+// capture can continue, move i of the masks is move i of the list (from, to,
+// captured squares) and the counts agree.  *simple counts those boards,
+// *captures the ones among them that capture.  Returns the number of boards
+// that differ.
+long rh_simple_moves_match_enum(uint64_t n, uint64_t seed, uint64_t *simple, uint64_t *captures) {
+  uint64_t x = seed;
+  auto next = [&]() {
+    uint64_t z = (x += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+  };
+  long bad = 0;
+  uint64_t ns = 0, nc = 0;
+  for (uint64_t t = 0; t < n; t++) {
+    uint32_t occ = (uint32_t)next() & (uint32_t)next();
+    if (t & 1) occ |= (uint32_t)next() & (uint32_t)next();
+    const uint32_t side = (uint32_t)next();
+    const uint32_t kmask = t % 3 == 0 ? (uint32_t)next() : (t % 3 == 1 ? 0u : (uint32_t)next() & (uint32_t)next());
+    const Board b = {occ & side, occ & ~side, occ & kmask, (uint32_t)(next() & 1)};
+    Side sd;
+    make_side(b, sd);
+    uint32_t M[4];
+    bool capture = false;
+    if (!simple_move_masks(sd, M, capture)) continue;
+    ns++;
+    nc += capture ? 1u : 0u;
+    const int k = popc(M[0]) + popc(M[1]) + popc(M[2]) + popc(M[3]);
+    int i = 0;
+    bool differ = false;
+    const int listed = for_each_move(sd, jumpers(sd), [&](int from, int to, uint32_t removed, int, uint32_t) {
+      int f = -1, o = -1;
+      uint32_t r = 0;
+      if (i < k) nth_move(M[0], M[1], M[2], M[3], (uint32_t)i, capture, sd.own & ~sd.ownK, f, o, r);
+      if (f != from || o != to || r != removed) differ = true;
+      i++;
+      return false;
+    });
+    if (differ || listed != k) bad++;
+  }
+  if (simple) *simple = ns;
+  if (captures) *captures = nc;
+  return bad;
+}
+}

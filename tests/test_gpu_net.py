@@ -7,6 +7,7 @@ import numpy as np
 import pytest
 
 import oracle_lib as L
+from gpu_ai_gb300 import GpuAIError
 from oracle import mlp
 
 pytestmark = pytest.mark.gpu
@@ -119,6 +120,38 @@ def test_train_step_is_adam_on_the_gradient(Net):
     want, _, _ = mlp.adam(p.astype(np.float64), 0.0, 0.0, g.astype(np.float64), step=1, lr=1e-3)
     assert np.abs(net.params() - want).max() < 1e-6
     net.close()
+
+
+def test_graph_replays_take_each_steps_rows_and_learning_rate(Net):
+    """The training step is one CUDA graph replayed step after step; a replay
+    on other rows (other device addresses) with another learning rate is Adam
+    step 2 on those rows' gradient at that rate, from step 1's parameters and
+    moments."""
+    net, grad = Net(0, max_batch=256, seed=1), Net(0, max_batch=256, seed=2)
+    p0 = _params(12)
+    net.set_params(p0)
+    rng = np.random.default_rng(4)
+    rows = []
+    for seed in (51, 52):
+        boards, _, _, _ = _positions(seed, 192)
+        rows.append((boards, rng.uniform(-1, 1, 192).astype(np.float32),
+                     rng.uniform(-1, 1, (192, mlp.MAXM)).astype(np.float32)))
+    dev = [_device_rows(*r) for r in rows]
+    assert dev[0][0].data_ptr() != dev[1][0].data_ptr()
+    g1, _ = net.gradients(*rows[0])
+    net.train_step(*(t.data_ptr() for t in dev[0]), 192, lr=1e-3)
+    p1 = net.params()
+    want1, m1, v1 = mlp.adam(p0.astype(np.float64), 0.0, 0.0, g1.astype(np.float64), step=1, lr=1e-3)
+    assert np.abs(p1 - want1).max() < 1e-6
+    grad.set_params(p1)
+    g2, _ = grad.gradients(*rows[1])
+    net.train_step(*(t.data_ptr() for t in dev[1]), 192, lr=3e-4)
+    want2, _, _ = mlp.adam(p1.astype(np.float64), m1, v1, g2.astype(np.float64), step=2, lr=3e-4)
+    assert np.abs(net.params() - want2).max() < 1e-6
+    with pytest.raises(GpuAIError):  # rows not 16-byte aligned
+        net.train_step(dev[0][0].data_ptr() + 4, dev[0][1].data_ptr(), dev[0][2].data_ptr(), 100, lr=1e-3)
+    net.close()
+    grad.close()
 
 
 def test_training_is_reproducible_and_resumable(Net, tmp_path):

@@ -166,3 +166,15 @@ def test_one_step_per_move_reference_heuristic_equals_enumeration(rh):
     rh.rh_heur_fast_matches_enum.restype = ctypes.c_long
     rh.rh_heur_fast_matches_enum.argtypes = [ctypes.c_uint64, ctypes.c_uint64]
     assert rh.rh_heur_fast_matches_enum(300_000, 23) == 0
+
+
+def test_simple_move_masks_list_the_moves_in_order(rh):
+    """The per-lane move list of the network kernels (simple_move_masks +
+    nth_move, for positions where no capture can continue) gives move i of
+    the reference list order on 1 M random boards, single jumps included."""
+    rh.rh_simple_moves_match_enum.restype = ctypes.c_long
+    rh.rh_simple_moves_match_enum.argtypes = [ctypes.c_uint64, ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64),
+                                              ctypes.POINTER(ctypes.c_uint64)]
+    simple, captures = ctypes.c_uint64(), ctypes.c_uint64()
+    assert rh.rh_simple_moves_match_enum(1_000_000, 29, ctypes.byref(simple), ctypes.byref(captures)) == 0
+    assert simple.value > 500_000 and captures.value > 50_000
