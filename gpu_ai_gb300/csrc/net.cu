@@ -17,8 +17,8 @@
 // Training step on a batch of B rows (a multiple of 128; rows past n are zero):
 //   features      X (B x 192), X^T
 //   F1  X  W1^T  -> H1 = bf16(relu(. + b1)), H1^T
-//   F2  H1 W2^T  -> H2 = bf16(relu(. + b2)), H2^T, vraw = H2 . wv + bv
-//   F3  H2 W3^T  -> logits = . + b3 (FP32)
+//   F2  H1 W2^T  -> H2 = bf16(relu(. + b2)), H2^T, H2 . wv over each 128-column tile
+//   F3  H2 W3^T  -> logits = . + b3 (FP32); vraw = the two tiles' sums + bv
 //   loss          dZ3 = (softmax - target) / n on the legal (from, to), dZ3^T, dv
 //   B1  dZ3 W3   -> dZ2 = bf16((. + dv wv^T) * [H2 > 0]), dZ2^T
 //   B3  dZ2 W2   -> dZ1^T = bf16(. * [H1 > 0])
@@ -74,7 +74,7 @@ struct gpuai_net {
   std::vector<void *> allocs;
   float *params = nullptr, *adam_m = nullptr, *adam_v = nullptr, *grad = nullptr;
   bf16 *W1b = nullptr, *W2b = nullptr, *W3b = nullptr, *W2T = nullptr, *W3T = nullptr;
-  CUtensorMap mW1, mW2, mW3, mW2T, mW3T;
+  CUtensorMap mW1, mW2, mW3, mW2T, mW3T, mW2Tn, mW3Tn;  // ..Tn: 64-row boxes
   uint64_t step = 0;
   ga::net::Fwd fw;
   bf16 *Xt = nullptr, *H1t = nullptr, *H2t = nullptr, *dZ3 = nullptr, *dZ3t = nullptr, *dZ2 = nullptr,
@@ -115,8 +115,9 @@ enum : uint32_t {
   kEpiB16T = 16u,     // BF16 transposed store: out_t[col * ld_t + row]
   kEpiMask = 32u,     // * [mask[row][col] > 0] (mask: BF16 ReLU output)
   kEpiRank1 = 64u,    // + r1_row[row] * r1_col[col]
-  kEpiVdot = 128u,    // vdot_out[row] = sum_col bf16(.) * vdot_w[col] + vdot_b (needs the whole row in one tile)
-  kEpiPartial = 256u  // FP32 row-major store into split-K partial blockIdx.z
+  kEpiVdot = 128u,    // vdot_part[blockIdx.y][row] = sum over the tile's columns of bf16(.) * vdot_w[col]
+  kEpiPartial = 256u, // FP32 row-major store into split-K partial blockIdx.z
+  kEpiVsum = 512u     // vdot_out[row] = (vdot_part[0][row] + vdot_part[1][row]) + vdot_b (first column tile)
 };
 
 struct Epi {
@@ -134,6 +135,8 @@ struct Epi {
   const float *r1_row = nullptr, *r1_col = nullptr;
   const float *vdot_w = nullptr, *vdot_b = nullptr;
   float *vdot_out = nullptr;
+  float *vdot_part = nullptr;  // [2][vdot_ld] per-tile partial sums of the value head
+  uint32_t vdot_ld = 0;
 };
 
 struct GemmArgs {
@@ -406,8 +409,10 @@ __global__ void __launch_bounds__(kThreads, 2)
 
   tc::fence_before_sync();
   __syncthreads();
-  if ((g.e.flags & kEpiVdot) && half == 0 && row_ok)  // the row's two column halves, in order
-    g.e.vdot_out[row] = vpart[trow] + vpart[kBM + trow] + g.e.vdot_b[0];
+  if ((g.e.flags & kEpiVdot) && half == 0 && row_ok)  // the tile's two column halves, in order
+    g.e.vdot_part[(size_t)blockIdx.y * g.e.vdot_ld + row] = vpart[trow] + vpart[kBM + trow];
+  if ((g.e.flags & kEpiVsum) && blockIdx.y == 0 && half == 0 && row_ok)  // the two tiles' sums, in order
+    g.e.vdot_out[row] = (g.e.vdot_part[row] + g.e.vdot_part[g.e.vdot_ld + row]) + g.e.vdot_b[0];
   if (*s_err) {
     if (threadIdx.x == 0) {
       atomicOr(g.status, kStatusNetWait);
@@ -863,7 +868,7 @@ cudaError_t gemm(const CUtensorMap &a, const CUtensorMap &b, uint32_t m_rows, ui
                  cudaStream_t s, bool pdl = false, uint64_t wait_ns = tc::kWaitLimitNs, bool skip_loads = false) {
   if (m_rows % kBM || bn % 64 || bn == 0 || bn > 256 || n_total % bn || splits == 0 || kb_total % splits)
     return cudaErrorInvalidValue;
-  if ((e.flags & kEpiVdot) && n_total != bn) return cudaErrorInvalidValue;  // the value head needs whole rows
+  if ((e.flags & kEpiVdot) && n_total != 2 * bn) return cudaErrorInvalidValue;  // the value head's two tiles
   GemmArgs g;
   g.m_rows = m_rows;
   g.bn = bn;
@@ -898,7 +903,10 @@ uint32_t pick_splits(uint32_t kb, uint32_t target) {
 
 constexpr uint32_t kSplit3 = 8, kSplit2 = 32, kSplit1 = 16;
 // N tile of each product (the B operand's tensor-map box height)
-constexpr uint32_t kBnF1 = 128, kBnF2 = 256 /* value head: whole rows */, kBnF3 = 256, kBnB1 = 128, kBnB3 = 128,
+// B1 and B3 take 128-wide tiles when that fills the SMs, else 64-wide (twice
+// the CTAs, two per SM); F2 takes two 128-wide tiles per row block, whose
+// value-head sums F3 adds.
+constexpr uint32_t kBnF1 = 128, kBnF2 = 128, kBnF3 = 256, kBnB1 = 128, kBnB3 = 128, kBnNarrow = 64,
                    kBnB2 = 128, kBnB4 = 128, kBnB5 = 64;
 
 template <class T>
@@ -924,6 +932,7 @@ cudaError_t fwd_alloc(Fwd &w, uint32_t rows, std::vector<void *> &allocs, bool b
   if (e == cudaSuccess && bf16_logits) e = dalloc(allocs, &w.logits_b, (size_t)w.rows * kOut);
   if (e == cudaSuccess && !bf16_logits) e = dalloc(allocs, &w.logits, (size_t)w.rows * kOut);
   if (e == cudaSuccess) e = dalloc(allocs, &w.vraw, (size_t)w.rows);
+  if (e == cudaSuccess) e = dalloc(allocs, &w.vpart, 2 * (size_t)w.rows);
   if (e == cudaSuccess) e = make_map(&w.mX, w.X, w.rows, kInPad, kBM);
   if (e == cudaSuccess) e = make_map(&w.mH1, w.H1, w.rows, kH, kBM);
   if (e == cudaSuccess) e = make_map(&w.mH2, w.H2, w.rows, kH, kBM);
@@ -956,13 +965,17 @@ cudaError_t forward_impl(const gpuai_net *net, Fwd &w, const gpuai_board *boards
   e2.out_b = w.H2;
   e2.out_t = net->H2t;
   e2.vdot_w = P + oWV;
-  e2.vdot_b = P + oBV;
-  e2.vdot_out = w.vraw;
+  e2.vdot_part = w.vpart;
+  e2.vdot_ld = w.rows;
   if ((e = gemm(w.mH1, net->mW2, rows, kH, kBnF2, kH / kBK, 1, dev_n, status, e2, s, train)) != cudaSuccess)
     return e;
   Epi e3;
-  e3.flags = kEpiBias | (w.logits_b ? kEpiB16 : kEpiF32);
+  e3.flags = kEpiBias | kEpiVsum | (w.logits_b ? kEpiB16 : kEpiF32);
   e3.bias = P + oB3;
+  e3.vdot_part = w.vpart;
+  e3.vdot_ld = w.rows;
+  e3.vdot_b = P + oBV;
+  e3.vdot_out = w.vraw;
   e3.out_f32 = w.logits;
   e3.ld_f32 = kOut;
   e3.out_b = w.logits_b;
@@ -1015,8 +1028,9 @@ cudaError_t backward_impl(gpuai_net *net, const gpuai_board *boards, const float
   b1.ld_b = kH;
   b1.out_t = net->dZ2t;
   b1.ld_t = L;
-  if ((e = gemm(net->mdZ3, net->mW3T, B, kH, kBnB1, kOut / kBK, 1, nullptr, net->status, b1, s, true)) !=
-      cudaSuccess)
+  const bool wide = (B / kBM) * (kH / kBnB1) >= sm_count();  // 128-wide tiles of B1 and B3 fill the SMs
+  if ((e = gemm(net->mdZ3, wide ? net->mW3T : net->mW3Tn, B, kH, wide ? kBnB1 : kBnNarrow, kOut / kBK, 1, nullptr,
+                net->status, b1, s, true)) != cudaSuccess)
     return e;
   // third stream, after dZ2: dW2 partials and db2; side stream: dZ3 (read
   // by dZ2's product) and dZ3^T (dW3's) back to zero, which nothing in the
@@ -1043,8 +1057,8 @@ cudaError_t backward_impl(gpuai_net *net, const gpuai_board *boards, const float
   b3.ld_mask = kH;
   b3.out_t = net->dZ1t;
   b3.ld_t = L;
-  if ((e = gemm(net->mdZ2, net->mW2T, B, kH, kBnB3, kH / kBK, 1, nullptr, net->status, b3, s, true)) !=
-      cudaSuccess)
+  if ((e = gemm(net->mdZ2, wide ? net->mW2T : net->mW2Tn, B, kH, wide ? kBnB3 : kBnNarrow, kH / kBK, 1, nullptr,
+                net->status, b3, s, true)) != cudaSuccess)
     return e;
   // third stream, after dZ1: db1; then the main stream waits for both side streams
   if ((e = cudaEventRecord(net->ev_b3, s)) != cudaSuccess) return e;
@@ -1277,6 +1291,8 @@ int gpuai_net_create(int device, uint32_t max_batch, uint64_t init_seed, gpuai_n
   if (e == cudaSuccess) e = make_map(&net->mW3, net->W3b, kOut, kH, kBnF3);
   if (e == cudaSuccess) e = make_map(&net->mW2T, net->W2T, kH, kH, kBnB3);
   if (e == cudaSuccess) e = make_map(&net->mW3T, net->W3T, kH, kOut, kBnB1);
+  if (e == cudaSuccess) e = make_map(&net->mW2Tn, net->W2T, kH, kH, kBnNarrow);
+  if (e == cudaSuccess) e = make_map(&net->mW3Tn, net->W3T, kH, kOut, kBnNarrow);
   if (e == cudaSuccess) e = make_map(&net->mXt, net->Xt, kInPad, L, kBnB5);
   if (e == cudaSuccess) e = make_map(&net->mH1t, net->H1t, kH, L, kBnB4);
   if (e == cudaSuccess) e = make_map(&net->mH2t, net->H2t, kH, L, kBnB2);

@@ -42,6 +42,7 @@ struct Fwd {
   __nv_bfloat16 *X = nullptr, *H1 = nullptr, *H2 = nullptr;
   float *logits = nullptr, *vraw = nullptr;  // FP32 logits (training, host forward) ...
   __nv_bfloat16 *logits_b = nullptr;         // ... or BF16 logits (search leaves: priors only)
+  float *vpart = nullptr;                    // [2][rows] value-head sums of F2's two column tiles
   CUtensorMap mX, mH1, mH2;
 };
 
