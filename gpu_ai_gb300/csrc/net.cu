@@ -901,7 +901,14 @@ uint32_t pick_splits(uint32_t kb, uint32_t target) {
   return 1;
 }
 
+// Split-K factors of the weight-gradient products (K = the batch): dW3, dW2,
+// dW1 above 16,384 rows; up to 16,384 rows dW1 takes more splits (more CTAs
+// for the last product of the chain) and dW2 fewer (fewer partials for Adam
+// to sum), 2 % faster at 8192 rows and 0.7 % slower at 32,768.
 constexpr uint32_t kSplit3 = 8, kSplit2 = 32, kSplit1 = 16;
+constexpr uint32_t kSmallBatch = 16384, kSplit2Small = 16, kSplit1Small = 32;
+constexpr uint32_t kMaxSplit2 = kSplit2 > kSplit2Small ? kSplit2 : kSplit2Small;
+constexpr uint32_t kMaxSplit1 = kSplit1 > kSplit1Small ? kSplit1 : kSplit1Small;
 // N tile of each product (the B operand's tensor-map box height)
 // B1 and B3 take 128-wide tiles when that fills the SMs, else 64-wide (twice
 // the CTAs, two per SM); F2 takes two 128-wide tiles per row block, whose
@@ -999,9 +1006,10 @@ cudaError_t backward_impl(gpuai_net *net, const gpuai_board *boards, const float
                   net->fw.vraw, net->dZ3, net->dZ3t, L, net->dv, net->rowloss)) != cudaSuccess)
     return e;
   const uint32_t kb = B / kBK;
+  const bool small = B <= kSmallBatch;
   splits[2] = pick_splits(kb, kSplit3);
-  splits[1] = pick_splits(kb, kSplit2);
-  splits[0] = pick_splits(kb, kSplit1);
+  splits[1] = pick_splits(kb, small ? kSplit2Small : kSplit2);
+  splits[0] = pick_splits(kb, small ? kSplit1Small : kSplit1);
   const cudaStream_t t = net->side, u = net->side2;
   // side stream, after the loss: dW3 partials, db3, dwv, the loss means and dbv
   if ((e = cudaEventRecord(net->ev_loss, s)) != cudaSuccess) return e;
@@ -1279,8 +1287,8 @@ int gpuai_net_create(int device, uint32_t max_batch, uint64_t init_seed, gpuai_n
   if (e == cudaSuccess) e = dalloc(A, &net->loss2, 2);
   if (e == cudaSuccess) e = dalloc(A, &net->value, L);
   if (e == cudaSuccess) e = dalloc(A, &net->p3, (size_t)kSplit3 * kOut * kH);
-  if (e == cudaSuccess) e = dalloc(A, &net->p2, (size_t)kSplit2 * kH * kH);
-  if (e == cudaSuccess) e = dalloc(A, &net->p1, (size_t)kSplit1 * kH * kInPad);
+  if (e == cudaSuccess) e = dalloc(A, &net->p2, (size_t)kMaxSplit2 * kH * kH);
+  if (e == cudaSuccess) e = dalloc(A, &net->p1, (size_t)kMaxSplit1 * kH * kInPad);
   if (e == cudaSuccess) e = dalloc(A, &net->status, 1);
   if (e == cudaSuccess) e = dalloc(A, &net->in_boards, L);
   if (e == cudaSuccess) e = dalloc(A, &net->in_z, L);
