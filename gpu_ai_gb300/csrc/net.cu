@@ -11,8 +11,11 @@
 // issues tcgen05.mma (M = 128, N = BN, K = 16 per instruction, FP32
 // accumulators in TMEM), then all eight warps read the accumulators back
 // (warp w owns TMEM lanes 32(w%4).. , i.e. 32 tile rows, and half of the
-// columns) and apply a fused epilogue.  The ring is sized so that two CTAs fit
-// on an SM: one CTA's epilogue overlaps the other's loads and MMAs.
+// columns) and apply a fused epilogue, whose stores go through a per-warp
+// staging area in the (by then idle) ring so that every store instruction
+// writes whole sectors.  The ring is sized so that two CTAs fit on an SM: one
+// CTA's epilogue overlaps the other's loads and MMAs; a product of the
+// training chain whose grid is at most one CTA per SM gets twice the ring.
 //
 // Training step on a batch of B rows (a multiple of 128; rows past n are zero):
 //   features      X (B x 192), X^T
