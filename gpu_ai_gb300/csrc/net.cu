@@ -77,7 +77,7 @@ struct gpuai_net {
   std::vector<void *> allocs;
   float *params = nullptr, *adam_m = nullptr, *adam_v = nullptr, *grad = nullptr;
   bf16 *W1b = nullptr, *W2b = nullptr, *W3b = nullptr, *W2T = nullptr, *W3T = nullptr;
-  CUtensorMap mW1, mW2, mW3, mW2T, mW3T, mW2Tn, mW3Tn;  // ..Tn: 64-row boxes
+  CUtensorMap mW1, mW2, mW3, mW2T, mW3T, mW2Tn, mW3Tn, mW2w;  // ..Tn: 64-row boxes; mW2w: 256-row boxes
   uint64_t step = 0;
   ga::net::Fwd fw;
   bf16 *Xt = nullptr, *H1t = nullptr, *H2t = nullptr, *dZ3 = nullptr, *dZ3t = nullptr, *dZ2 = nullptr,
@@ -118,7 +118,7 @@ enum : uint32_t {
   kEpiB16T = 16u,     // BF16 transposed store: out_t[col * ld_t + row]
   kEpiMask = 32u,     // * [mask[row][col] > 0] (mask: BF16 ReLU output)
   kEpiRank1 = 64u,    // + r1_row[row] * r1_col[col]
-  kEpiVdot = 128u,    // vdot_part[blockIdx.y][row] = sum over the tile's columns of bf16(.) * vdot_w[col]
+  kEpiVdot = 128u,    // vdot_part[t][row] = sum over columns 128t .. 128t+127 of bf16(.) * vdot_w[col]
   kEpiPartial = 256u, // FP32 row-major store into split-K partial blockIdx.z
   kEpiVsum = 512u     // vdot_out[row] = (vdot_part[0][row] + vdot_part[1][row]) + vdot_b (first column tile)
 };
@@ -399,21 +399,28 @@ __global__ void __launch_bounds__(kThreads, 2)
   const bool warp_ok = __all_sync(0xffffffffu, *s_err == 0u);
   const bool row_ok = row < rows && warp_ok;
   uint8_t *stage = smem + warp * kStageBytesPerWarp;  // the ring is free: every MMA has read its stage
-  float vsum = 0.0f;
+  // value head: one FP32 chain per 64 columns (the first and the second 64
+  // of a 128-column half-tile), so that a 128-column tile's sum is the same
+  // whether the tile is a CTA of its own (two warp halves) or half of a
+  // 256-column CTA (one warp half)
+  float vs0 = 0.0f, vs1 = 0.0f;
   const uint32_t c_lo = half * (bn / 2), c_hi = c_lo + bn / 2;
   for (uint32_t c = c_lo; c < c_hi; c += 32) {
     float v[32];
     tc::tmem_load32(tmem + ((quad * 32u) << 16) + c, v);  // warp-collective: every lane takes part
     const uint32_t col0 = blockIdx.y * bn + c;
     if (row_ok) epilogue_math(g.e, v, row, col0);
-    if (warp_ok) epilogue_store(g.e, v, stage, row0 + quad * 32u, rows, lane, col0, blockIdx.z, vsum);
+    if (warp_ok)
+      epilogue_store(g.e, v, stage, row0 + quad * 32u, rows, lane, col0, blockIdx.z, c - c_lo < 64u ? vs0 : vs1);
   }
-  if (g.e.flags & kEpiVdot) vpart[half * kBM + trow] = vsum;
+  if (g.e.flags & kEpiVdot) vpart[half * kBM + trow] = vs0;
 
   tc::fence_before_sync();
   __syncthreads();
-  if ((g.e.flags & kEpiVdot) && half == 0 && row_ok)  // the tile's two column halves, in order
-    g.e.vdot_part[(size_t)blockIdx.y * g.e.vdot_ld + row] = vpart[trow] + vpart[kBM + trow];
+  if ((g.e.flags & kEpiVdot) && row_ok) {  // each 128-column tile: its two 64-column chains, in order
+    if (bn == 256u) g.e.vdot_part[(size_t)half * g.e.vdot_ld + row] = vs0 + vs1;
+    else if (half == 0) g.e.vdot_part[(size_t)blockIdx.y * g.e.vdot_ld + row] = vpart[trow] + vpart[kBM + trow];
+  }
   if ((g.e.flags & kEpiVsum) && blockIdx.y == 0 && half == 0 && row_ok)  // the two tiles' sums, in order
     g.e.vdot_out[row] = (g.e.vdot_part[row] + g.e.vdot_part[g.e.vdot_ld + row]) + g.e.vdot_b[0];
   if (*s_err) {
@@ -585,6 +592,117 @@ __global__ void loss_kernel(const gpuai_board *boards, const float *z, const flo
     for (int o = 16; o; o >>= 1) ce += __shfl_xor_sync(kFull, ce, o);
   }
   if (lane == 0) rowloss[2 * r] = ce;
+}
+
+// The terms of loss_kernel for row r on a segment of W lanes of the warp:
+// lane l of the segment holds move l of the row's list (pair pi) or none, k
+// moves in all; the segment's first lane writes the row's terms.  Same
+// arithmetic as loss_kernel's (its 32-lane reductions only add the neutral
+// values of lanes without a move).  Warp-collective: every lane of the warp
+// calls it, with W = 32 (one row) or W = 16 (two rows, one per half).
+template <uint32_t W>
+__device__ __forceinline__ void row_loss(uint32_t r, bool row_ok, int k, uint32_t pi, const float *z, const float *q,
+                                         uint32_t n, float tau, float vcoef, const float *logits, const float *vraw,
+                                         bf16 *dZ3, bf16 *dZ3t, uint32_t ldt, float *dv, float *rowloss) {
+  constexpr uint32_t kFull = 0xffffffffu;
+  const uint32_t lane = threadIdx.x & 31u, sl = lane & (W - 1u), base = lane & ~(W - 1u);
+  const float inv_n = 1.0f / (float)n;
+  if (sl == 0) {
+    float dvr = 0.0f, ve = 0.0f;
+    if (row_ok) {
+      const float th = tanhf(vraw[r]);
+      const float e = th - z[r];
+      dvr = vcoef * 2.0f * e * (1.0f - th * th) * inv_n;
+      ve = e * e;
+    }
+    dv[r] = dvr;
+    rowloss[2 * r + 1] = ve;
+  }
+  const bool act = row_ok && k >= 1 && k <= (int)kMaxMoves && sl < (uint32_t)k;
+  const float qm = act ? q[(size_t)r * kMaxMoves + sl] : -3.0e38f;
+  float qmax = qm;
+  for (uint32_t o = W / 2; o; o >>= 1) qmax = fmaxf(qmax, __shfl_xor_sync(kFull, qmax, o));
+  const float et = act ? expf((qm - qmax) / tau) : 0.0f;
+  float tsum = et;
+  for (uint32_t o = W / 2; o; o >>= 1) tsum += __shfl_xor_sync(kFull, tsum, o);
+  const float t = act ? et / tsum : 0.0f;
+  const uint32_t grp = __match_any_sync(kFull, pi | (base << 20));  // pairs of the lane's own row
+  const bool leader = act && (uint32_t)(__ffs(grp) - 1) == lane;
+  float tp = t;  // target of this lane's pair: sum over the lanes sharing it, in lane order
+  if (__any_sync(kFull, (grp & (grp - 1u)) != 0u)) {  // some pair has two moves (king captures)
+    tp = 0.0f;
+    for (uint32_t j = 0; j < W; j++) {
+      const float tj = __shfl_sync(kFull, t, base + j);
+      if ((grp >> (base + j)) & 1u) tp += tj;
+    }
+  }
+  const float lg = leader ? logits[(size_t)r * kOut + pi] : -3.0e38f;
+  float lmax = lg;
+  for (uint32_t o = W / 2; o; o >>= 1) lmax = fmaxf(lmax, __shfl_xor_sync(kFull, lmax, o));
+  float sum = leader ? expf(lg - lmax) : 0.0f;
+  for (uint32_t o = W / 2; o; o >>= 1) sum += __shfl_xor_sync(kFull, sum, o);
+  float ce = 0.0f;
+  if (leader) {
+    const float lp = lg - (lmax + logf(sum));
+    ce = -tp * lp;
+    const bf16 gq = __float2bfloat16_rn((expf(lp) - tp) * inv_n);
+    dZ3[(size_t)r * kOut + pi] = gq;
+    dZ3t[(size_t)pi * ldt + r] = gq;
+  }
+  for (uint32_t o = W / 2; o; o >>= 1) ce += __shfl_xor_sync(kFull, ce, o);
+  if (sl == 0) rowloss[2 * r] = ce;
+}
+
+// loss_kernel for batches of several waves of warps, two rows per warp (rows
+// 2w and 2w+1): when both list at most 16 moves, none of them a capture that
+// can continue, each half of the warp takes one row and each lane its move
+// straight from the move masks; otherwise the warp takes the two rows one
+// after the other on all 32 lanes.  Half the warps and about half the
+// instructions of one row per warp, which pays where the rows fill several
+// waves; where they fit in one, loss_kernel's shorter warps are faster.
+__global__ void loss_pairs_kernel(const gpuai_board *boards, const float *z, const float *q, uint32_t n,
+                                  uint32_t rows, float tau, float vcoef, const float *logits, const float *vraw,
+                                  bf16 *dZ3, bf16 *dZ3t, uint32_t ldt, float *dv, float *rowloss) {
+  tc::grid_dep_wait();  // the logits and the value come from the kernel before this one
+  tc::grid_dep_trigger();
+  constexpr uint32_t kFull = 0xffffffffu;
+  const uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31u;
+  const uint32_t r0 = 2u * w;
+  if (r0 >= rows) return;  // uniform over the warp; rows is even
+  const uint32_t r = r0 + (lane >> 4), hl = lane & 15u;
+  Side sd{};
+  uint32_t M[4] = {0u, 0u, 0u, 0u};
+  bool capture = false, simple = true;
+  int k = 0;
+  if (r < n) {
+    const uint4 bv = __ldg(reinterpret_cast<const uint4 *>(boards) + r);
+    make_side(Board{bv.x, bv.y, bv.z, bv.w}, sd);
+    simple = simple_move_masks(sd, M, capture);
+    k = simple ? popc(M[0]) + popc(M[1]) + popc(M[2]) + popc(M[3]) : 0;
+  }
+  if (__all_sync(kFull, simple && k <= 16)) {
+    uint32_t pi = 0x10000u + lane;  // distinct placeholder for lanes without a move
+    if (hl < (uint32_t)k) {
+      int from, to;
+      uint32_t removed;
+      nth_move(M[0], M[1], M[2], M[3], hl, capture, sd.own & ~sd.ownK, from, to, removed);
+      pi = (uint32_t)(from * 32 + to);
+    }
+    row_loss<16>(r, r < n, k, pi, z, q, n, tau, vcoef, logits, vraw, dZ3, dZ3t, ldt, dv, rowloss);
+    return;
+  }
+  for (uint32_t h = 0; h < 2; h++) {
+    const uint32_t rr = r0 + h;
+    int kk = 0;
+    uint32_t pi = 0x10000u + lane;
+    if (rr < n) {
+      const uint4 bv = __ldg(reinterpret_cast<const uint4 *>(boards) + rr);
+      Side s2;
+      make_side(Board{bv.x, bv.y, bv.z, bv.w}, s2);
+      pi = lane_pair(s2, jumpers(s2), kk, lane, 0x10000u + lane);
+    }
+    row_loss<32>(rr, rr < n, kk, pi, z, q, n, tau, vcoef, logits, vraw, dZ3, dZ3t, ldt, dv, rowloss);
+  }
 }
 
 // Zeroes the entries of dZ3 and dZ3^T that loss_kernel wrote for rows [0, n):
@@ -871,7 +989,8 @@ cudaError_t gemm(const CUtensorMap &a, const CUtensorMap &b, uint32_t m_rows, ui
                  cudaStream_t s, bool pdl = false, uint64_t wait_ns = tc::kWaitLimitNs, bool skip_loads = false) {
   if (m_rows % kBM || bn % 64 || bn == 0 || bn > 256 || n_total % bn || splits == 0 || kb_total % splits)
     return cudaErrorInvalidValue;
-  if ((e.flags & kEpiVdot) && n_total != 2 * bn) return cudaErrorInvalidValue;  // the value head's two tiles
+  if ((e.flags & kEpiVdot) && !(n_total == 256u && (bn == 128u || bn == 256u)))  // the value head's two tiles
+    return cudaErrorInvalidValue;
   GemmArgs g;
   g.m_rows = m_rows;
   g.bn = bn;
@@ -914,8 +1033,9 @@ constexpr uint32_t kMaxSplit2 = kSplit2 > kSplit2Small ? kSplit2 : kSplit2Small;
 constexpr uint32_t kMaxSplit1 = kSplit1 > kSplit1Small ? kSplit1 : kSplit1Small;
 // N tile of each product (the B operand's tensor-map box height)
 // B1 and B3 take 128-wide tiles when that fills the SMs, else 64-wide (twice
-// the CTAs, two per SM); F2 takes two 128-wide tiles per row block, whose
-// value-head sums F3 adds.
+// the CTAs, two per SM); F2 takes two 128-wide tiles per row block while
+// that leaves SMs idle, else one 256-wide tile (the value-head sums of its two
+// halves are the same either way, and F3 adds them).
 constexpr uint32_t kBnF1 = 128, kBnF2 = 128, kBnF3 = 256, kBnB1 = 128, kBnB3 = 128, kBnNarrow = 64,
                    kBnB2 = 128, kBnB4 = 128, kBnB5 = 64;
 
@@ -977,7 +1097,11 @@ cudaError_t forward_impl(const gpuai_net *net, Fwd &w, const gpuai_board *boards
   e2.vdot_w = P + oWV;
   e2.vdot_part = w.vpart;
   e2.vdot_ld = w.rows;
-  if ((e = gemm(w.mH1, net->mW2, rows, kH, kBnF2, kH / kBK, 1, dev_n, status, e2, s, train)) != cudaSuccess)
+  // F2 in 128-column tiles (two CTAs per row block) while that leaves SMs
+  // idle, in 256-column tiles once the row blocks alone fill the SMs
+  const bool wide2 = rows / kBM >= sm_count();
+  if ((e = gemm(w.mH1, wide2 ? net->mW2w : net->mW2, rows, kH, wide2 ? 2u * kBnF2 : kBnF2, kH / kBK, 1, dev_n, status,
+                e2, s, train)) != cudaSuccess)
     return e;
   Epi e3;
   e3.flags = kEpiBias | kEpiVsum | (w.logits_b ? kEpiB16 : kEpiF32);
@@ -1005,8 +1129,12 @@ cudaError_t backward_impl(gpuai_net *net, const gpuai_board *boards, const float
   // the one before it drains (programmatic dependent launch); dZ3 and dZ3^T
   // are zero on entry apart from what this step's loss kernel writes.
   net->dz_dirty = true;  // until clear_dz3_kernel is queued
-  if ((e = launch(loss_kernel, dim3(B / 4), 128, 0, s, true, boards, z, q, n, B, tau, vcoef, net->fw.logits,
-                  net->fw.vraw, net->dZ3, net->dZ3t, L, net->dv, net->rowloss)) != cudaSuccess)
+  // one row per warp while the rows fit one wave of resident warps (64 per
+  // SM with these 128-thread blocks), two per warp above that
+  const bool pairs = B > 64u * sm_count();
+  if ((e = launch(pairs ? loss_pairs_kernel : loss_kernel, dim3(pairs ? B / 8 : B / 4), 128, 0, s, true, boards, z,
+                  q, n, B, tau, vcoef, net->fw.logits, net->fw.vraw, net->dZ3, net->dZ3t, L, net->dv,
+                  net->rowloss)) != cudaSuccess)
     return e;
   const uint32_t kb = B / kBK;
   const bool small = B <= kSmallBatch;
@@ -1299,6 +1427,7 @@ int gpuai_net_create(int device, uint32_t max_batch, uint64_t init_seed, gpuai_n
   if (e != cudaSuccess) return fail(cuda_err(e, "gpuai_net_create: allocation"));
   e = make_map(&net->mW1, net->W1b, kH, kInPad, kBnF1);
   if (e == cudaSuccess) e = make_map(&net->mW2, net->W2b, kH, kH, kBnF2);
+  if (e == cudaSuccess) e = make_map(&net->mW2w, net->W2b, kH, kH, 2u * kBnF2);
   if (e == cudaSuccess) e = make_map(&net->mW3, net->W3b, kOut, kH, kBnF3);
   if (e == cudaSuccess) e = make_map(&net->mW2T, net->W2T, kH, kH, kBnB3);
   if (e == cudaSuccess) e = make_map(&net->mW3T, net->W3T, kH, kOut, kBnB1);
@@ -1505,7 +1634,9 @@ int gpuai_net_train_step(gpuai_net *net, const gpuai_board *d_boards, const floa
     const cudaError_t ec = cudaStreamEndCapture(s, &g);
     if (e == cudaSuccess) e = ec;
     if (e == cudaSuccess) e = find_kernel_node(g, (const void *)features_kernel, &net->node_features);
-    if (e == cudaSuccess) e = find_kernel_node(g, (const void *)loss_kernel, &net->node_loss);
+    if (e == cudaSuccess)
+      e = find_kernel_node(g, round128(n) > 64u * sm_count() ? (const void *)loss_pairs_kernel : (const void *)loss_kernel,
+                           &net->node_loss);
     if (e == cudaSuccess) e = find_kernel_node(g, (const void *)clear_dz3_kernel, &net->node_clear);
     if (e == cudaSuccess) e = find_kernel_node(g, (const void *)adam_kernel, &net->node_adam);
     if (e == cudaSuccess) e = cudaGraphInstantiate(&net->train_graph, g, 0);

@@ -7,6 +7,7 @@ import numpy as np
 import pytest
 
 import oracle_lib as L
+from golden_boards import random_boards
 from gpu_ai_gb300 import GpuAIError
 from oracle import mlp
 
@@ -94,6 +95,58 @@ def test_gradients_match_oracle(Net, n, tau, vc):
         err = np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-12)
         assert err < 2e-2, f"{name}: relative error {err:.3g}"
     assert np.all(g[mlp.O_W1:mlp.O_B1].reshape(mlp.H, mlp.IN_PAD)[:, mlp.IN:] == 0)
+    net.close()
+
+
+def test_gradients_with_two_rows_per_loss_warp(Net):
+    """Batches larger than one wave of loss warps put two rows in a warp (one
+    per half, each lane's move from the move masks).  1024 positions repeated
+    16 times (16384 rows: two per warp) give the gradient of the 1024 alone
+    (one per warp): the mean over rows is the same and 16 is a power of two,
+    so every row's BF16 gradient scales exactly; what remains is the order of
+    the FP32 sums.  A row whose moves were mapped wrongly would be off by
+    about 1/1024 of the affected entries."""
+    net = Net(0, max_batch=16384, seed=1)
+    net.set_params(_params(7))
+    boards, _, _, counts = _positions(61, 768)
+    # random placements with kings: longer move lists and continuing captures
+    extra = random_boards(np.random.default_rng(8), 4000)
+    extra[:, 3] &= np.uint32(1)  # no draw counter
+    _, c = L.genmoves(extra)
+    extra = extra[(c > 0) & (c <= mlp.MAXM)][:256]
+    boards = np.concatenate([boards, extra])
+    _, counts = L.genmoves(boards)
+
+    def continues(x):  # some legal move takes two or more pieces
+        side = int(x[3]) & 1
+        opp = int(x[1 - side])
+        return any(bin(opp & ~int(c[1 - side])).count("1") >= 2 for c in L.children(x)[0])
+
+    whole = np.array([continues(x) for x in boards]) | (counts > 16)  # rows a warp takes on all 32 lanes
+    assert len(boards) == 1024 and 50 < whole.sum() < 512
+    rng = np.random.default_rng(7)
+    z = rng.uniform(-1, 1, 1024).astype(np.float32)
+    q = rng.uniform(-1, 1, (1024, mlp.MAXM)).astype(np.float32)
+    g1, l1 = net.gradients(boards, z, q)
+    g16, l16 = net.gradients(np.tile(boards, (16, 1)), np.tile(z, 16), np.tile(q, (16, 1)))
+    for name, (lo, hi) in _segments().items():
+        a, b = g1[lo:hi], g16[lo:hi]
+        assert np.abs(a - b).max() <= 1e-4 * max(np.abs(a).max(), 1e-12), name
+    assert np.allclose(l1, l16, rtol=1e-5)
+    net.close()
+
+
+def test_forward_is_the_same_for_both_tile_widths_of_the_second_layer(Net):
+    """A batch whose row blocks fill the SMs runs the second layer in
+    256-column tiles, a smaller one in 128-column tiles; values (whose
+    dot product is summed per 64 columns either way) and logits of the same
+    boards are bit-identical."""
+    net = Net(0, max_batch=20480, seed=1)
+    net.set_params(_params(5))
+    boards = L.random_positions(17, 20000, 0, 60)
+    v_big, l_big = net.forward(boards)
+    v_small, l_small = net.forward(boards[:300])
+    assert np.array_equal(v_big[:300], v_small) and np.array_equal(l_big[:300], l_small)
     net.close()
 
 
