@@ -705,7 +705,8 @@ __global__ void loss_pairs_kernel(const gpuai_board *boards, const float *z, con
   }
 }
 
-// Zeroes the entries of dZ3 and dZ3^T that loss_kernel wrote for rows [0, n):
+// Zeroes the entries of dZ3 and dZ3^T that the loss (loss_kernel or
+// loss_pairs_kernel) wrote for rows [0, n):
 // the (from, to) pairs of each row's legal moves, found the same way.
 __global__ void clear_dz3_kernel(const gpuai_board *boards, uint32_t n, bf16 *dZ3, bf16 *dZ3t, uint32_t ldt) {
   const uint32_t r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31u;
